@@ -1,0 +1,279 @@
+"""Benchmark: Alpha158 fp32 factor-graph batch run (KunQuant runGraph) on GB300.
+
+Workload (default): the Alpha158 factor graph (158 outputs from OHLCV+amount),
+fp32, [T][S] layout, 5000 stocks x 2500 days of seeded synthetic OHLCV with
+0.5% NaN cells.  One step = one runGraph over the whole batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  `value` is stock-days/s with the inputs resident on the
+GPU; `e2e` is the same through the C ABI with pinned host buffers (host->device
+inputs and device->host outputs inside the timed region).  The reference arm
+(`--impl reference`) times the CPU restatement of the reference executor (the
+oracle) on the host cores, on a bounded sample.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+WORKLOADS = {
+    "alpha158": dict(key="alpha158_f32", module="alpha158", stocks=5000, days=2500, nan=0.005,
+                     n_inputs=6, n_outputs=158),
+    "alpha101": dict(key="alpha101_f32", module="alpha101", stocks=64, days=260, nan=0.0,
+                     n_inputs=6, n_outputs=82),
+}
+
+
+def _dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def _peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for n, v in zip(names, r[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def cpu_reference(workload: dict, steps: int, warmup: int, seconds_target: float = 15.0):
+    """The reference executor's algorithm on the host cores (the oracle port),
+    on a bounded sample of the workload: all stocks, a slice of the days."""
+    from kunquant_gb300 import synth
+    from kunquant_gb300.graph import predefined_spec
+    from oracle.oracle import OracleProgram
+    prog = OracleProgram(predefined_spec(workload["key"]))
+    threads = os.cpu_count() or 1
+    S = workload["stocks"]
+    # calibrate the slice so a step takes a few seconds
+    days = min(workload["days"], 100)
+    data = synth.ohlcv(S, days, seed=7, nan_frac=workload["nan"])
+    t0 = time.perf_counter()
+    prog.run(data, nthreads=threads)
+    dt = time.perf_counter() - t0
+    per_sd = dt / (S * days)
+    budget = seconds_target / max(1, steps + warmup)
+    days = int(min(workload["days"], max(50, budget / per_sd / S)))
+    data = synth.ohlcv(S, days, seed=7, nan_frac=workload["nan"])
+    for _ in range(warmup):
+        prog.run(data, nthreads=threads)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        prog.run(data, nthreads=threads)
+    dt = (time.perf_counter() - t0) / steps
+    return {"value": S * days / dt, "unit": "stock-days/s", "cores": threads, "kind": "port",
+            "sample": f"{S} stocks x {days} days of the same seeded OHLCV, {steps} timed runs",
+            "s_per_step": dt}
+
+
+def stage_bytes(mod_spec, stage_idx, S, T, elem):
+    st = mod_spec["stages"][stage_idx]
+    return (len(set(st["in"])) + len(st["out"])) * S * T * elem
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="alpha158", choices=sorted(WORKLOADS))
+    ap.add_argument("--stocks", type=int, default=None)
+    ap.add_argument("--days", type=int, default=None)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    wl = dict(WORKLOADS[args.workload])
+    if args.stocks:
+        wl["stocks"] = args.stocks
+    if args.days:
+        wl["days"] = args.days
+    world, rank, local = _dist_env()
+    config = {"workload": f"{args.workload} fp32 TS, {wl['stocks']} stocks x {wl['days']} days, "
+                          f"{wl['nan'] * 100:.1f}% NaN cells",
+              "module": wl["key"], "stocks": wl["stocks"], "days": wl["days"],
+              "l2": "inputs (6 x S x T x 4 B) exceed the 129 MB L2; no flush"}
+    metric = "stock-days/s"
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        ref = cpu_reference(wl, args.steps, args.warmup)
+        line = {"metric": metric, "value": ref["value"], "unit": "stock-days/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ref["s_per_step"] * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config, "impl": "reference",
+                "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": ref["value"], "unit": "stock-days/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    from kunquant_gb300 import runner as kr
+    from kunquant_gb300 import synth
+    from kunquant_gb300.graph import predefined_spec
+    spec = predefined_spec(wl["key"])
+    S, T = wl["stocks"], wl["days"]
+    lib = kr.Library.predefined(wl["key"])
+    mod = lib.getModule(wl["module"])
+    data = synth.ohlcv(S, T, seed=1234 + rank, nan_frac=wl["nan"])
+    dev_in = {k: torch.from_numpy(v).cuda() for k, v in data.items()}
+    dev_out = {n: torch.empty((T, S), dtype=torch.float32, device="cuda") for n in mod.getOutputNames()}
+    ex = kr.createSingleThreadExecutor()
+
+    def step():
+        kr.runGraph(ex, mod, dev_in, 0, T, outputs=dev_out)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    ex.set_profiling(True)
+    stage_ms = {}
+    sampler = ClockSampler(torch.cuda.current_device())
+    sampler.start()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        step()
+        for sid, ms in ex.stage_times():
+            stage_ms.setdefault(sid, []).append(ms)
+        launches += ex.last_launch_count()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop()
+    ex.set_profiling(False)
+    ms_step = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_step = float(t.item())
+    value = world * S * T / (ms_step / 1e3)
+
+    # dominant kernel and its HBM roofline
+    avg = {sid: float(np.mean(v)) for sid, v in stage_ms.items()}
+    top = max(avg, key=avg.get)
+    elem = 4
+    alg_bytes = stage_bytes(spec, top, S, T, elem)
+    achieved = alg_bytes / (avg[top] / 1e3) / 1e9
+    peak, peak_kind = _peaks()
+    traffic = None
+    tf = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            traffic = json.load(f).get(f"{wl['key']}:{top}")
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
+                "kernel": f"stage {top} of {wl['key']} ({avg[top]:.3f} ms/launch, "
+                          f"{100 * avg[top] / sum(avg.values()):.1f}% of kernel time)",
+                "whole_step_frac": (wl["n_inputs"] + wl["n_outputs"]) * S * T * elem / (ms_step / 1e3) / 1e9 / peak}
+
+    # end to end through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        host_in = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in data.items()}
+        host_out = {n: torch.empty((T, S), dtype=torch.float32).pin_memory().numpy()
+                    for n in mod.getOutputNames()}
+        kr.runGraph(ex, mod, host_in, 0, T, outputs=host_out)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            kr.runGraph(ex, mod, host_in, 0, T, outputs=host_out)
+        dt = (time.perf_counter() - t0) / args.steps
+        e2e = {"value": world * S * T / dt, "unit": "stock-days/s",
+               "h2d_bytes_per_step": wl["n_inputs"] * S * T * elem,
+               "d2h_bytes_per_step": len(host_out) * S * T * elem, "ms_per_step": dt * 1e3}
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        ref = cpu_reference(wl, 2, 1, seconds_target=12.0)
+        cpu = {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        line = {"metric": metric, "value": value, "unit": "stock-days/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic", "config": config, "roofline": roofline, "cpu_baseline": cpu,
+                "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+                "stage_ms": {str(k): round(v, 4) for k, v in sorted(avg.items(), key=lambda x: -x[1])[:8]}}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,155 @@
+/*
+ * kun_gpu.h -- C ABI of the GB300 backend of KunQuant.
+ *
+ * Drop-in for the reference C API (cpp/Kun/CApi.h): the same handles, the same
+ * function names and argument meanings, so a C/Go/Rust/ctypes binding written
+ * for KunQuant links against libkungpu.so unchanged.  Differences:
+ *   - an "executor" is a CUDA execution context on the current device (one or
+ *     more CUDA streams) instead of a CPU thread pool;
+ *   - a "library" is a module library produced by the GPU code generator
+ *     (kunquant_gb300.jit.compileit or the prebuilt Alpha101/Alpha158 ones);
+ *   - buffers given to kunSetBufferNameMap may be host or device pointers;
+ *     host buffers are copied to the device and back inside kunRunGraph;
+ *   - every call reports errors through its return status and
+ *     kunGetLastError() instead of C++ exceptions.
+ * Functions below marked "GPU extension" have no counterpart in CApi.h.
+ */
+#ifndef KUN_GPU_H
+#define KUN_GPU_H
+#include <stddef.h>
+#include <stdint.h>
+
+typedef void *KunExecutorHandle;
+typedef void *KunLibraryHandle;
+typedef void *KunModuleHandle;
+typedef void *KunBufferNameMapHandle;
+typedef void *KunStreamContextHandle;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KUN_API_VERSION 1
+
+/* cpp/Kun/CApi.h:17-21 */
+typedef enum {
+    KUN_INIT_NONE = 0,
+    KUN_INIT_FILE,
+    KUN_INIT_MEMORY,
+} KunStateBufferKind;
+
+/* cpp/Kun/CApi.h:23-27, extended with GPU failure codes */
+typedef enum {
+    KUN_SUCCESS = 0,
+    KUN_INIT_ERROR,
+    KUN_INVALID_ARGUMENT,
+    KUN_CUDA_ERROR,
+    KUN_OUT_OF_MEMORY,
+    KUN_TIMEOUT,
+} KunStatus;
+
+/* cpp/Kun/CApi.h:29-40 */
+typedef struct {
+    size_t version;
+    KunStateBufferKind init_kind;
+    union {
+        const char *path;
+        struct {
+            const char *buffer;
+            size_t size;
+        } memory;
+    } init;
+} KunStreamExtraArgs;
+
+/* Replaces kunCreateSingleThreadExecutor (cpp/Kun/CApi.h:48): a GPU executor
+ * on the current CUDA device with one stream. */
+KunExecutorHandle kunCreateSingleThreadExecutor(void);
+/* Replaces kunCreateMultiThreadExecutor (cpp/Kun/CApi.h:57): `numthreads` is
+ * the number of CUDA streams used to run independent stages concurrently. */
+KunExecutorHandle kunCreateMultiThreadExecutor(int numthreads);
+/* cpp/Kun/CApi.h:65 (sic: "Destory" as in the reference) */
+void kunDestoryExecutor(KunExecutorHandle ptr);
+
+/* cpp/Kun/CApi.h:73: load a GPU module library (.so) */
+KunLibraryHandle kunLoadLibrary(const char *path_or_name);
+/* cpp/Kun/CApi.h:82: borrowed handle, never freed */
+KunModuleHandle kunGetModuleFromLibrary(KunLibraryHandle lib, const char *name);
+/* cpp/Kun/CApi.h:90 */
+void kunUnloadLibrary(KunLibraryHandle ptr);
+
+/* cpp/Kun/CApi.h:98-125 */
+KunBufferNameMapHandle kunCreateBufferNameMap(void);
+void kunDestoryBufferNameMap(KunBufferNameMapHandle ptr);
+void kunSetBufferNameMap(KunBufferNameMapHandle ptr, const char *name, float *buffer);
+void kunEraseBufferNameMap(KunBufferNameMapHandle ptr, const char *name);
+
+/* cpp/Kun/CApi.h:144: run the batch graph and wait for it.  Inputs are
+ * [total_time][num_stocks] (TS) or [num_stocks/blocking][total_time][blocking]
+ * (STs); outputs have `length` rows starting at `cur_time`.  Errors are
+ * reported through kunGetLastError(). */
+void kunRunGraph(KunExecutorHandle exec, KunModuleHandle m, KunBufferNameMapHandle buffers,
+                 size_t num_stocks, size_t total_time, size_t cur_time, size_t length);
+
+/* cpp/Kun/CApi.h:153-170 */
+KunStreamContextHandle kunCreateStream(KunExecutorHandle exec, KunModuleHandle m, size_t num_stocks);
+KunStatus kunCreateStreamEx(KunExecutorHandle exec, KunModuleHandle m, size_t num_stocks,
+                            const KunStreamExtraArgs *extra_args, KunStreamContextHandle *out_handle);
+/* cpp/Kun/CApi.h:190: two-phase size query as in the reference */
+KunStatus kunStreamSerializeStates(KunStreamContextHandle context, KunStateBufferKind dump_kind,
+                                   char *path_or_buffer, size_t *size);
+/* cpp/Kun/CApi.h:205 */
+size_t kunQueryBufferHandle(KunStreamContextHandle context, const char *name);
+/* cpp/Kun/CApi.h:216: host copy of the buffer's current row, valid until the
+ * next kunStreamPushData / kunStreamRun */
+const float *kunStreamGetCurrentBuffer(KunStreamContextHandle context, size_t handle);
+/* cpp/Kun/CApi.h:227: host data, num_stocks values */
+void kunStreamPushData(KunStreamContextHandle context, size_t handle, const float *buffer);
+/* cpp/Kun/CApi.h:235 */
+void kunStreamRun(KunStreamContextHandle context);
+/* cpp/Kun/CApi.h:241 */
+void kunDestoryStream(KunStreamContextHandle context);
+
+/* ---------------- GPU extensions ---------------- */
+
+/* Status-returning kunRunGraph.  With `synchronize` = 0 and device buffers the
+ * call only enqueues work on the executor's stream (and may be captured into
+ * a CUDA graph). */
+KunStatus kunRunGraphEx(KunExecutorHandle exec, KunModuleHandle m, KunBufferNameMapHandle buffers,
+                        size_t num_stocks, size_t total_time, size_t cur_time, size_t length,
+                        int synchronize);
+/* Make the executor enqueue on an existing CUDA stream (cudaStream_t), e.g.
+ * the caller's current stream; NULL restores the executor's own stream. */
+KunStatus kunExecutorSetStream(KunExecutorHandle exec, void *cuda_stream);
+KunStatus kunExecutorSynchronize(KunExecutorHandle exec);
+/* Record a CUDA event after every stage launch of the following runs (1) or
+ * stop (0); kunExecutorStageTimes returns the per-stage milliseconds of the
+ * last run (stage ids in launch order), or -1 when profiling is off. */
+KunStatus kunExecutorSetProfiling(KunExecutorHandle exec, int enable);
+int kunExecutorStageTimes(KunExecutorHandle exec, int32_t *stage_ids, float *ms, int cap);
+/* Count of kernel launches of the last run (for instrumentation). */
+int64_t kunExecutorLastLaunchCount(KunExecutorHandle exec);
+/* Text of the last error of the calling thread ("" if none). */
+const char *kunGetLastError(void);
+
+/* Module metadata (cpp/Python/PyBinding.cpp:182-221 exposes the same). */
+int kunModuleNumBuffers(KunModuleHandle m);
+const char *kunModuleBufferName(KunModuleHandle m, int idx);
+int kunModuleBufferKind(KunModuleHandle m, int idx);        /* 0 input, 1 output, 2 temp */
+int kunModuleBufferUnreliableCount(KunModuleHandle m, int idx);
+int kunModuleBufferWindow(KunModuleHandle m, int idx);
+int kunModuleInputLayout(KunModuleHandle m);                /* 0 STs, 1 TS, 2 STREAM */
+int kunModuleOutputLayout(KunModuleHandle m);
+int kunModuleBlockingLen(KunModuleHandle m);
+int kunModuleDtype(KunModuleHandle m);                      /* 0 float, 1 double */
+int kunModuleNumStages(KunModuleHandle m);
+
+/* Stream sessions on device buffers (GPU extension of the stream API):
+ * push a device row / read the device pointer of the current row. */
+KunStatus kunStreamPushDataDevice(KunStreamContextHandle context, size_t handle, const void *device_buffer);
+const void *kunStreamGetCurrentBufferDevice(KunStreamContextHandle context, size_t handle);
+KunStatus kunStreamRunEx(KunStreamContextHandle context, int synchronize);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,375 @@
+// Device templates of the GPU backend: the arithmetic of KunQuant's op
+// templates (cpp/Kun/Ops.hpp, cpp/Kun/Ops/Quantile.hpp, cpp/Kun/Rank.hpp,
+// cpp/Kun/Scale.hpp, cpp/KunSIMD/cpu/Math.hpp) written for one stock per
+// thread.  Every translation unit that includes this file is compiled with
+// -fmad=false: a product is fused into an add only where a template below
+// calls kfma(), which is exactly where the reference's GCC build forms an FMA.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace kun {
+
+template <typename T> struct FpBits;
+template <> struct FpBits<float> {
+    using U = uint32_t;
+    using S = int32_t;
+    static constexpr int mant = 23;
+    static constexpr int expo = 8;
+};
+template <> struct FpBits<double> {
+    using U = unsigned long long;
+    using S = long long;
+    static constexpr int mant = 52;
+    static constexpr int expo = 11;
+};
+
+__device__ __forceinline__ uint32_t kbits(float x) { return __float_as_uint(x); }
+__device__ __forceinline__ unsigned long long kbits(double x) {
+    return (unsigned long long)__double_as_longlong(x);
+}
+__device__ __forceinline__ float kfrom(uint32_t u, float) { return __uint_as_float(u); }
+__device__ __forceinline__ double kfrom(unsigned long long u, double) {
+    return __longlong_as_double((long long)u);
+}
+template <typename T> __device__ __forceinline__ T knan() {
+    return kfrom((typename FpBits<T>::U)(sizeof(T) == 4 ? 0x7fc00000ull : 0x7ff8000000000000ull), T());
+}
+template <typename T> __device__ __forceinline__ T kinf() {
+    return kfrom((typename FpBits<T>::U)(sizeof(T) == 4 ? 0x7f800000ull : 0x7ff0000000000000ull), T());
+}
+// boolean results are all-ones / all-zeros bit masks, as SIMD compares produce
+template <typename T> __device__ __forceinline__ T kmask(bool b) {
+    using U = typename FpBits<T>::U;
+    return kfrom(b ? (U)~(U)0 : (U)0, T());
+}
+// blend by the sign bit of the condition (_mm256_blendv_ps semantics)
+template <typename T> __device__ __forceinline__ bool ksel(T c) {
+    using U = typename FpBits<T>::U;
+    return (kbits(c) >> (sizeof(U) * 8 - 1)) != 0;
+}
+template <typename T> __device__ __forceinline__ bool kisnan(T x) { return x != x; }
+
+__device__ __forceinline__ float kfma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double kfma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float kadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double kadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float ksub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double ksub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float kmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double kmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float kdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double kdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float ksqrt(float a) { return __fsqrt_rn(a); }
+__device__ __forceinline__ double ksqrt(double a) { return __dsqrt_rn(a); }
+__device__ __forceinline__ float kfloor(float a) { return floorf(a); }
+__device__ __forceinline__ double kfloor(double a) { return floor(a); }
+
+template <typename T> __device__ __forceinline__ T kmax(T a, T b) { return a > b ? a : b; }
+template <typename T> __device__ __forceinline__ T kmin(T a, T b) { return a < b ? a : b; }
+template <typename T> __device__ __forceinline__ T kabs(T a) {
+    using U = typename FpBits<T>::U;
+    return kfrom(kbits(a) & (((U)~(U)0) >> 1), T());
+}
+template <typename T> __device__ __forceinline__ T kor(T a, T b) { return kfrom(kbits(a) | kbits(b), T()); }
+template <typename T> __device__ __forceinline__ T kand(T a, T b) { return kfrom(kbits(a) & kbits(b), T()); }
+template <typename T> __device__ __forceinline__ T knot(T a) { return kfrom(~kbits(a), T()); }
+template <typename T> __device__ __forceinline__ T kselect(T c, T a, T b) { return ksel(c) ? a : b; }
+
+// Sign, cpp/Kun/Ops.hpp:692-701
+template <typename T> __device__ __forceinline__ T ksign(T v) {
+    T r = kisnan(v) ? knan<T>() : T(1);
+    r = v < T(0) ? T(-1) : r;
+    r = v == T(0) ? T(0) : r;
+    return r;
+}
+// SetInfOrNanToValue, cpp/Kun/Ops.hpp:715-720
+template <typename T> __device__ __forceinline__ T ksetinfnan(T a, T v) {
+    T d = ksub(a, a);
+    return kisnan(d) ? v : a;
+}
+
+// Table-driven log of cpp/KunSIMD/cpu/Math.hpp:20-93.  The reciprocal and
+// log tables are supplied by the generated code (kLogR<T>, kLogLR<T>) as
+// exact binary literals.
+template <typename T> struct LogTables;
+
+template <typename T> __device__ __forceinline__ T klogfast(T x) {
+    using U = typename FpBits<T>::U;
+    using S = typename FpBits<T>::S;
+    constexpr int mb = FpBits<T>::mant, eb = FpBits<T>::expo;
+    U xi = kbits(x);
+    U high5 = (xi >> (mb - 5)) & (U)31;
+    U high1 = high5 >> 4;
+    U e1 = (high1 ^ (((U)1 << (eb - 1)) - 1)) << mb;
+    U m = (xi & ((((U)1) << mb) - 1)) | e1;
+    T ri = LogTables<T>::r(high5);
+    // the reference build contracts `Ri * M - 1` and both uses of `poly * Z`
+    T z = kfma(ri, kfrom(m, T()), T(-1.0));
+    T poly = T(1 / 5.0);
+    poly = kfma(poly, z, T(-1 / 4.0));
+    poly = kfma(poly, z, T(1 / 3.0));
+    poly = kfma(poly, z, T(-1 / 2.0));
+    poly = kfma(poly, z, T(1.0));
+    T mlog = LogTables<T>::lr(high5);
+    U er = (xi >> mb) + high1;
+    T ep = (T)(S)er;
+    T v2 = kfma(ep, T(0.6931471805599453), mlog);
+    T hi = kfma(poly, z, v2);
+    T lo = ksub(hi, v2);
+    lo = kfma(-poly, z, lo);
+    hi = kadd(hi, lo);
+    if (x == T(0)) hi = -kinf<T>();
+    if (x < T(0)) hi = knan<T>();
+    if (x == kinf<T>()) hi = kinf<T>();
+    if (kisnan(x)) hi = knan<T>();
+    if (x == T(1.0)) hi = T(0);
+    return hi;
+}
+
+// exp of cpp/KunSIMD/cpu/Math.hpp:96-140 (float thresholds for both types)
+template <typename T> __device__ __forceinline__ T kexpk(T x) {
+    using U = typename FpBits<T>::U;
+    using S = typename FpBits<T>::S;
+    T k = kfloor(kfma(x, T(1.4426950408889634), T(0.5)));
+    S ki = (kisnan(k) || k > T(1e9) || k < T(-1e9)) ? (S)0 : (S)k;
+    T r = kfma(-k, T(0.6931471805599453), x);
+    T tn = kfma(r, T(0.16666666666666666), T(1.0));
+    tn = kfma(tn, kmul(r, T(0.2)), T(1.0));
+    tn = kfma(tn, kmul(r, T(0.25)), T(1.0));
+    tn = kfma(tn, kmul(r, T(0.3333333333333333)), T(1.0));
+    tn = kfma(tn, kmul(r, T(0.5)), T(1.0));
+    tn = kfma(tn, r, T(1.0));
+    U p = ((U)ki) << FpBits<T>::mant;
+    T res = kfrom(p + kbits(tn), T());
+    if (x > T(88.72283935)) res = kinf<T>();
+    if (x < T(-87.33654785)) res = T(0);
+    return res;
+}
+
+// ---------------- reductions of a back-window loop, cpp/Kun/Ops.hpp:468-616
+template <typename T> struct RAdd {
+    T v = 0, c = 0;
+    __device__ __forceinline__ void step(T x) {
+        T y = ksub(x, c);
+        T t = kadd(v, y);
+        c = ksub(ksub(t, v), y);
+        v = t;
+    }
+    // input is a product a*b contracted into `y = a*b - c`
+    __device__ __forceinline__ void step_fma(T a, T b) {
+        T y = kfma(a, b, -c);
+        T t = kadd(v, y);
+        c = ksub(ksub(t, v), y);
+        v = t;
+    }
+    // first step of a loop the reference build unrolls completely: with
+    // v = c = 0 folded in, the product feeds both `0 + p` and `t - p`
+    __device__ __forceinline__ void step_fma_first(T a, T b) {
+        T t = kfma(a, b, v);
+        c = kfma(-a, b, ksub(t, v));
+        v = t;
+    }
+    __device__ __forceinline__ T value() const { return v; }
+};
+template <typename T> struct RMul {
+    T v = T(1.0);
+    __device__ __forceinline__ void step(T x) { v = kmul(v, x); }
+    __device__ __forceinline__ T value() const { return v; }
+};
+template <typename T> struct RMin {
+    T v = kinf<T>();
+    __device__ __forceinline__ void step(T x) { v = (kisnan(v) || kisnan(x)) ? knan<T>() : kmin(v, x); }
+    __device__ __forceinline__ T value() const { return v; }
+};
+template <typename T> struct RMax {
+    T v = -kinf<T>();
+    __device__ __forceinline__ void step(T x) { v = (kisnan(v) || kisnan(x)) ? knan<T>() : kmax(v, x); }
+    __device__ __forceinline__ T value() const { return v; }
+};
+template <typename T, bool IsMax> struct RArg {
+    T v = IsMax ? -kinf<T>() : kinf<T>();
+    T idx = 0;
+    __device__ __forceinline__ void step(T x, int iter) {
+        bool isn = kisnan(v) || kisnan(x);
+        bool cmp = IsMax ? (v < x) : (v > x);
+        v = cmp ? x : v;
+        v = isn ? knan<T>() : v;
+        idx = cmp ? T(iter) : idx;
+        idx = isn ? knan<T>() : idx;
+    }
+    __device__ __forceinline__ T value() const { return idx; }
+};
+template <typename T> struct RRank {
+    T v, less = 0, eq = 0;
+    __device__ __forceinline__ explicit RRank(T cur) : v(cur) {}
+    __device__ __forceinline__ void step(T x) {
+        bool isn = kisnan(v) || kisnan(x);
+        less = isn ? knan<T>() : less;
+        less = (x < v) ? kadd(less, T(1.0)) : less;
+        eq = (x == v) ? kadd(eq, T(1.0)) : eq;
+    }
+    __device__ __forceinline__ T value() const { return kadd(less, kdiv(kadd(eq, T(1.0)), T(2.0))); }
+};
+template <typename T, int W> struct RDecay {
+    static constexpr double kStep = 1.0 / ((1.0 + W) * W / 2);
+    T weight = T(kStep), v = 0;
+    __device__ __forceinline__ void step(T x) {
+        v = kfma(x, weight, v);
+        weight = kadd(weight, T(kStep));
+    }
+    __device__ __forceinline__ T value() const { return v; }
+};
+
+// ---------------- stateful ops carried over time
+// FastWindowedSum, cpp/Kun/Ops.hpp:324-356
+template <typename T> struct FWSum {
+    T v = 0, cadd = 0, csub = 0;
+    int nn;
+    __device__ __forceinline__ explicit FWSum(int window) : nn(window) {}
+    __device__ __forceinline__ T step(T old, T cur) {
+        bool on = kisnan(old), cn = kisnan(cur);
+        if (!on) {
+            T y = ksub(ksub(T(0), old), csub);
+            T t = kadd(v, y);
+            csub = ksub(ksub(t, v), y);
+            v = t;
+        }
+        if (!cn) {
+            T y = ksub(cur, cadd);
+            T t = kadd(v, y);
+            cadd = ksub(ksub(t, v), y);
+            v = t;
+        }
+        nn = nn - (int)on + (int)cn;
+        return nn == 0 ? v : knan<T>();
+    }
+};
+
+// ExpMovingAvg, cpp/Kun/Ops.hpp:358-375
+template <typename T, int W> struct EMA {
+    T v;
+    __device__ __forceinline__ explicit EMA(T init) : v(init) {}
+    __device__ __forceinline__ T step(T cur) {
+        const T w = kdiv(T(2.0), T(W + 1));
+        T nv = kfma(cur, w, kmul(v, ksub(T(1), w)));
+        T r = kisnan(cur) ? v : nv;
+        r = kisnan(v) ? cur : r;
+        v = r;
+        return r;
+    }
+};
+
+// WindowedLinearRegression, cpp/Kun/Ops.hpp:377-466
+template <typename T, int W> struct LinReg {
+    T isum = 0, xsum = 0, x2sum = 0, ysum = 0, y2sum = 0, xysum = 0;
+    int nn = W;
+    // SharedSq: cur*cur is shared with another regression of the stage in
+    // the reference build and is then not contracted
+    template <bool SharedSq>
+    __device__ __forceinline__ void step(T old, T cur) {
+        const T w = T(W);
+        xysum = ksub(xysum, ysum);
+        x2sum = ksub(kadd(x2sum, isum), kmul(T(2.0), xsum));
+        xsum = ksub(xsum, isum);
+        bool on = kisnan(old), cn = kisnan(cur);
+        if (!on) {
+            isum = ksub(isum, T(1));
+            ysum = ksub(ysum, old);
+            y2sum = kfma(-old, old, y2sum);
+        }
+        nn = nn - (int)on + (int)cn;
+        if (!cn) {
+            isum = kadd(isum, T(1));
+            xsum = kadd(xsum, w);
+            x2sum = kadd(x2sum, kmul(w, w));
+            ysum = kadd(ysum, cur);
+            y2sum = SharedSq ? kadd(y2sum, kmul(cur, cur)) : kfma(cur, cur, y2sum);
+            xysum = kfma(w, cur, xysum);
+        }
+    }
+    __device__ __forceinline__ T n() const { return (T)(W - nn); }
+    __device__ __forceinline__ T rsq() const {
+        T N = n();
+        T r1 = kfma(-xsum, ysum, kmul(N, xysum));
+        r1 = kmul(r1, r1);
+        T r2 = kmul(kfma(-xsum, xsum, kmul(N, x2sum)), kfma(-ysum, ysum, kmul(N, y2sum)));
+        return kdiv(r1, r2);
+    }
+    __device__ __forceinline__ T slope() const {
+        T N = n();
+        return kdiv(kfma(-xsum, ysum, kmul(N, xysum)), kfma(-xsum, xsum, kmul(N, x2sum)));
+    }
+    __device__ __forceinline__ T resi(T val) const {
+        T N = n();
+        T s = slope();
+        T xm = kdiv(xsum, N), ym = kdiv(ysum, N);
+        T interp = kfma(-s, xm, ym);
+        return ksub(val, kfma(s, T(W), interp));
+    }
+};
+
+// Order-statistic window of the skip-list ops (cpp/Kun/Ops/Quantile.hpp:16-170,
+// cpp/Kun/SkipList.cpp:125-273): the last `W` non-NaN values kept sorted, equal
+// values in insertion order.  Values are kept as double like the skip list.
+template <int W> struct SortedWindow {
+    double v[W + 1];
+    int idx[W + 1];
+    int size = 0;
+    int last_rank = 0;
+    __device__ __forceinline__ void remove(double x) {
+        int p = 0;
+        while (p < size && v[p] < x) p++;
+        if (p >= size || v[p] != x) return;
+        for (int j = p; j < size - 1; j++) { v[j] = v[j + 1]; idx[j] = idx[j + 1]; }
+        size--;
+    }
+    __device__ __forceinline__ int insert(double x, int index) {
+        int p = 0;
+        while (p < size && v[p] <= x) p++;
+        for (int j = size; j > p; j--) { v[j] = v[j - 1]; idx[j] = idx[j - 1]; }
+        v[p] = x;
+        idx[p] = index;
+        size++;
+        return p;
+    }
+    __device__ __forceinline__ int min_rank(double x) const {
+        int p = 0;
+        while (p < size && v[p] < x) p++;
+        return p;
+    }
+    template <typename T>
+    __device__ __forceinline__ void step(T oldv, T newv, int index) {
+        if (!kisnan(oldv)) remove((double)oldv);
+        if (!kisnan(newv)) last_rank = insert((double)newv, index);
+    }
+    template <typename T> __device__ __forceinline__ T quantile(T q) const {
+        if (size != W) return knan<T>();
+        T iwf = kmul(q, (T)(size - 1));
+        int id = (int)iwf;
+        if ((T)id == iwf) return (T)v[id];
+        double lo = v[id], hi = v[id + 1];
+        T frac = ksub(iwf, (T)id);
+        return (T)__fma_rn(__dsub_rn(hi, lo), (double)frac, lo);
+    }
+    template <typename T> __device__ __forceinline__ T vmin() const {
+        return size != W ? knan<T>() : (T)v[0];
+    }
+    template <typename T> __device__ __forceinline__ T vmax() const {
+        return size != W ? knan<T>() : (T)v[W - 1];
+    }
+    template <typename T> __device__ __forceinline__ T argmin(long long cur_idx) const {
+        if (size != W) return knan<T>();
+        return (T)(unsigned long long)((unsigned long long)idx[0] + (unsigned long long)size -
+                                       (unsigned long long)cur_idx);
+    }
+    template <typename T> __device__ __forceinline__ T rank(T cur) const {
+        if (size != W) return knan<T>();
+        double r = last_rank + 1;
+        double rmin = min_rank((double)cur) + 1;
+        r = (((r * (r + 1) / 2) - ((rmin - 1) * rmin / 2)) / (r - rmin + 1));
+        return (T)r;
+    }
+};
+
+}  // namespace kun

@@ -1,0 +1,79 @@
+// ABI between the runtime (libkungpu.so) and the module libraries the code
+// generator emits.  A module library exports one `KunGpuModuleDesc` per
+// module, named `kun_module_<module name>`; this mirrors the reference's
+// `Module` table (cpp/Kun/Module.hpp:16-28, cpp/Kun/Stage.hpp:26-66), with CUDA
+// launch functions in place of the CPU stage functions.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define KUN_GPU_MODULE_ABI 0x6b470002ull
+
+typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
+typedef enum { KUN_BUF_INPUT = 0, KUN_BUF_OUTPUT = 1, KUN_BUF_TEMP = 2 } KunGpuBufferKind;
+typedef enum { KUN_STAGE_TS = 0, KUN_STAGE_RANK = 1, KUN_STAGE_SCALE = 2, KUN_STAGE_XSEC = 3 } KunGpuStageKind;
+
+typedef struct {
+    int32_t id;
+    const char *name;
+    int32_t kind;              /* KunGpuBufferKind */
+    int32_t num_users;
+    int32_t unreliable_count;  /* rows at the start of a run that are not reliable */
+    int32_t window;            /* ring depth in stream mode */
+} KunGpuBufferDesc;
+
+/* Arguments of one stage launch.  `buffers` is indexed by module buffer id and
+ * holds device pointers; `scratch` holds the stage's private [length][S]
+ * device buffers (one per in-stage windowed temporary).  In stream mode
+ * `buffers[b]` points at buffer b's ring ([window][S]) and `ring_pos` at the
+ * per-buffer write positions. */
+typedef struct {
+    void *const *buffers;
+    void *const *scratch;
+    int64_t num_stocks;
+    int64_t total_time;
+    int64_t start;
+    int64_t length;
+    const int32_t *ring_pos;   /* stream mode only (host array) */
+    void *state;               /* stream mode: per-stage persistent op state (device) */
+    int32_t *error_flag;       /* device word; kernels set it instead of trapping */
+} KunGpuStageArgs;
+
+typedef int (*KunGpuLaunchFn)(const KunGpuStageArgs *args, void *cuda_stream);
+
+typedef struct {
+    const char *name;
+    int32_t kind;              /* KunGpuStageKind */
+    int32_t num_in;
+    const int32_t *in_bufs;
+    int32_t num_out;
+    const int32_t *out_bufs;
+    int32_t num_deps;          /* stages that depend on this one */
+    const int32_t *deps;
+    int32_t pending;           /* number of stages this one waits for */
+    int32_t num_scratch;       /* private [length][S] buffers needed */
+    int64_t state_bytes_per_stock; /* stream mode persistent state */
+    KunGpuLaunchFn launch;
+} KunGpuStageDesc;
+
+typedef struct {
+    uint64_t abi;              /* KUN_GPU_MODULE_ABI */
+    const char *name;
+    int32_t num_stages;
+    const KunGpuStageDesc *stages;
+    int32_t num_buffers;
+    const KunGpuBufferDesc *buffers;
+    int32_t input_layout;      /* KunGpuLayout */
+    int32_t output_layout;
+    int32_t blocking_len;
+    int32_t dtype;             /* 0 = float, 1 = double */
+    int32_t aligned;
+} KunGpuModuleDesc;
+
+#ifdef __cplusplus
+}
+#endif

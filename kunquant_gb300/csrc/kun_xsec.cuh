@@ -1,0 +1,199 @@
+// Cross-sectional kernels: one thread block per time step (row of the [T][S]
+// layout).
+//  - Rank (cpp/Kun/Rank.hpp:13-57): the row's non-NaN values are sorted in
+//    shared memory (bitonic network over order-preserving integer keys; NaNs
+//    sort last), then every stock binary-searches its equal range;
+//    out = T(sum) / T(cnt) / T(n) with the integer rank sum of the range.
+//  - Scale (cpp/Kun/Scale.hpp:14-46): the sum of |x| over non-NaN stocks in
+//    stock order (sequential, as the reference adds), then x / sum.
+//  - DiffWithWeightedSum (KunQuant/ops/MiscOp.py:220-240).
+#pragma once
+#include "kun_device.cuh"
+
+namespace kun {
+
+template <typename T> struct SortKey;
+template <> struct SortKey<float> {
+    using K = uint32_t;
+    static __device__ __forceinline__ K enc(float x) {
+        if (x != x) return 0xffffffffu;
+        uint32_t u = __float_as_uint(x);
+        return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+    }
+    static __device__ __forceinline__ float dec(K k) {
+        uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+        return __uint_as_float(u);
+    }
+    static constexpr K kMax = 0xffffffffu;
+};
+template <> struct SortKey<double> {
+    using K = unsigned long long;
+    static __device__ __forceinline__ K enc(double x) {
+        if (x != x) return ~0ull;
+        unsigned long long u = (unsigned long long)__double_as_longlong(x);
+        return (u & 0x8000000000000000ull) ? ~u : (u | 0x8000000000000000ull);
+    }
+    static __device__ __forceinline__ double dec(K k) {
+        unsigned long long u = (k & 0x8000000000000000ull) ? (k & 0x7fffffffffffffffull) : ~k;
+        return __longlong_as_double((long long)u);
+    }
+    static constexpr K kMax = ~0ull;
+};
+
+constexpr int kRankThreads = 1024;
+
+template <typename T>
+__global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ in, T *__restrict__ out,
+                                                          long long S, long long length, int P) {
+    using SK = SortKey<T>;
+    using K = typename SK::K;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    K *keys = reinterpret_cast<K *>(smem_raw);
+    __shared__ int cnt_warp[kRankThreads / 32];
+    const int tid = threadIdx.x;
+    for (long long t = blockIdx.x; t < length; t += gridDim.x) {
+        const T *row = in + t * S;
+        T *orow = out + t * S;
+        int local = 0;
+        for (int i = tid; i < P; i += blockDim.x) {
+            K k = SK::kMax;
+            if (i < S) {
+                T x = row[i];
+                k = SK::enc(x);
+                local += (x == x);
+            }
+            keys[i] = k;
+        }
+        for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+        if ((tid & 31) == 0) cnt_warp[tid >> 5] = local;
+        __syncthreads();
+        int n = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) n += cnt_warp[w];
+        for (int k = 2; k <= P; k <<= 1) {
+            for (int j = k >> 1; j > 0; j >>= 1) {
+                for (int i = tid; i < P; i += blockDim.x) {
+                    int ixj = i ^ j;
+                    if (ixj > i) {
+                        K a = keys[i], b = keys[ixj];
+                        bool up = (i & k) == 0;
+                        if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
+                    }
+                }
+                __syncthreads();
+            }
+        }
+        for (int i = tid; i < S; i += blockDim.x) {
+            T x = row[i];
+            T r;
+            if (x != x) {
+                r = knan<T>();
+            } else {
+                int lo = 0, hi = n;
+                while (lo < hi) { int m = (lo + hi) >> 1; if (SK::dec(keys[m]) < x) lo = m + 1; else hi = m; }
+                long long start = lo;
+                hi = n;
+                while (lo < hi) { int m = (lo + hi) >> 1; if (x < SK::dec(keys[m])) hi = m; else lo = m + 1; }
+                long long end = lo;
+                long long sum = (start + end + 1) * (end - start) / 2;
+                r = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
+            }
+            orow[i] = r;
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) scale_rows(const T *__restrict__ in, T *__restrict__ out, long long S,
+                                                  long long length) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *row_s = reinterpret_cast<T *>(smem_raw);
+    __shared__ T total;
+    for (long long t = blockIdx.x; t < length; t += gridDim.x) {
+        const T *row = in + t * S;
+        for (long long i = threadIdx.x; i < S; i += blockDim.x) row_s[i] = row[i];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            T sum = 0;
+            for (long long i = 0; i < S; i++) {
+                T x = row_s[i];
+                if (x == x) sum = kadd(sum, kabs(x));
+            }
+            total = sum;
+        }
+        __syncthreads();
+        T sum = total;
+        for (long long i = threadIdx.x; i < S; i += blockDim.x) {
+            T x = row_s[i];
+            out[t * S + i] = (x == T(0) && sum == T(0)) ? knan<T>() : kdiv(x, sum);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) diffwsum_rows(const T *__restrict__ in0, const T *__restrict__ in1,
+                                                    T *__restrict__ out, long long S, long long length) {
+    __shared__ T total;
+    for (long long t = blockIdx.x; t < length; t += gridDim.x) {
+        if (threadIdx.x == 0) {
+            T sum = 0;
+            // `sum += a * b` is contracted by the reference build
+            for (long long i = 0; i < S; i++) sum = kfma(in0[t * S + i], in1[t * S + i], sum);
+            total = sum;
+        }
+        __syncthreads();
+        T sum = total;
+        for (long long i = threadIdx.x; i < S; i += blockDim.x) out[t * S + i] = ksub(in0[t * S + i], sum);
+        __syncthreads();
+    }
+}
+
+inline int kun_num_sms() {
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 132;
+    }
+    return n;
+}
+
+template <typename T>
+inline int launch_rank(const T *in, T *out, long long S, long long length, cudaStream_t st) {
+    using K = typename SortKey<T>::K;
+    int P = 1;
+    while (P < S) P <<= 1;
+    size_t smem = (size_t)P * sizeof(K);
+    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(rank_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    long long grid = length < (long long)kun_num_sms() * 2 ? length : (long long)kun_num_sms() * 2;
+    rank_rows<T><<<(unsigned)grid, kRankThreads, smem, st>>>(in, out, S, length, P);
+    return (int)cudaGetLastError();
+}
+
+template <typename T>
+inline int launch_scale(const T *in, T *out, long long S, long long length, cudaStream_t st) {
+    size_t smem = (size_t)S * sizeof(T);
+    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(scale_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    long long grid = length < (long long)kun_num_sms() * 4 ? length : (long long)kun_num_sms() * 4;
+    scale_rows<T><<<(unsigned)grid, 256, smem, st>>>(in, out, S, length);
+    return (int)cudaGetLastError();
+}
+
+template <typename T>
+inline int launch_diffwsum(const T *in0, const T *in1, T *out, long long S, long long length, cudaStream_t st) {
+    long long grid = length < (long long)kun_num_sms() * 4 ? length : (long long)kun_num_sms() * 4;
+    diffwsum_rows<T><<<(unsigned)grid, 256, 0, st>>>(in0, in1, out, S, length);
+    return (int)cudaGetLastError();
+}
+
+}  // namespace kun

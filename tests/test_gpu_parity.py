@@ -1,0 +1,68 @@
+"""GPU vs oracle parity on the predefined factor libraries.
+
+The oracle restates the reference CPU executor (including the multiply-add
+contractions of its GCC build); the GPU path must reproduce it bit for bit.
+"""
+import numpy as np
+import pytest
+
+from kunquant_gb300 import runner as kr
+from kunquant_gb300 import synth
+from kunquant_gb300.graph import predefined_spec
+from oracle.oracle import OracleProgram
+from tests.parity import compare_exact
+
+CASES = [
+    # (library key, module name, stocks, days, nan fraction, cur_time)
+    ("alpha158_f32", "alpha158", 64, 260, 0.0, 0),
+    ("alpha158_f32", "alpha158", 61, 300, 0.005, 0),
+    ("alpha158_f32", "alpha158", 64, 260, 0.0, 50),
+    ("alpha101_f32", "alpha101", 64, 260, 0.0, 0),
+    ("alpha101_f32", "alpha101", 62, 260, 0.005, 0),
+    ("alpha101_f32", "alpha101", 64, 260, 0.0, 50),
+    ("alpha158_f64", "alpha158_f64", 32, 260, 0.005, 0),
+    ("alpha101_f64", "alpha101_f64", 32, 260, 0.005, 0),
+]
+
+_programs = {}
+_libs = {}
+
+
+def _oracle(key):
+    if key not in _programs:
+        _programs[key] = OracleProgram(predefined_spec(key))
+    return _programs[key]
+
+
+def _module(key, name):
+    if key not in _libs:
+        _libs[key] = kr.Library.predefined(key)
+    return _libs[key].getModule(name)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key,name,S,T,nanf,start", CASES)
+def test_numpy_path_bit_exact(key, name, S, T, nanf, start):
+    spec = predefined_spec(key)
+    dt = np.float32 if spec["dtype"] == "float" else np.float64
+    data = synth.ohlcv(S, T, seed=S * 7 + T, nan_frac=nanf, dtype=dt)
+    want = _oracle(key).run(data, cur_time=start, length=T - start)
+    ex = kr.createSingleThreadExecutor()
+    got = kr.runGraph(ex, _module(key, name), data, start, T - start)
+    bad = compare_exact(got, want)
+    assert not bad, f"{len(bad)} outputs differ: {dict(list(bad.items())[:5])}"
+
+
+@pytest.mark.gpu
+def test_torch_device_path_bit_exact():
+    import torch
+    key, name, S, T = "alpha158_f32", "alpha158", 128, 300
+    data = synth.ohlcv(S, T, seed=3, nan_frac=0.005)
+    want = _oracle(key).run(data)
+    ex = kr.createSingleThreadExecutor()
+    dev = {k: torch.from_numpy(v).cuda() for k, v in data.items()}
+    got = kr.runGraph(ex, _module(key, name), dev, 0, T)
+    torch.cuda.synchronize()
+    got = {k: v.cpu().numpy() for k, v in got.items()}
+    bad = compare_exact(got, want)
+    assert not bad, f"{len(bad)} outputs differ: {dict(list(bad.items())[:5])}"
