@@ -477,11 +477,25 @@ extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
         return src + launch, len(self.scratch)
 
 
+def stage_generator(spec: dict, si: int, tag: str, mode: str = "leveled") -> StageGen:
+    """Leveled kernels where the stage allows them, else the single-scan form."""
+    if mode == "leveled" and spec["stages"][si]["kind"] == "ts":
+        from .leveled import LeveledGen, Unsupported
+        try:
+            g = LeveledGen(spec, si, tag)
+            g.generate()  # dry run: fall back on anything the levels cannot express
+            return LeveledGen(spec, si, tag)
+        except Unsupported:
+            pass
+    return StageGen(spec, si, tag)
+
+
 def _c_str(s: str) -> str:
     return '"' + s.replace("\\", "\\\\").replace('"', '\\"') + '"'
 
 
-def generate_module(spec: dict, out_dir: str, tag: str = None, stages_per_file: int = 8) -> List[str]:
+def generate_module(spec: dict, out_dir: str, tag: str = None, stages_per_file: int = 8,
+                    mode: str = "leveled") -> List[str]:
     """Write the CUDA sources of one module; returns the list of .cu paths."""
     os.makedirs(out_dir, exist_ok=True)
     name = spec["name"]
@@ -515,7 +529,7 @@ template <> struct LogTables<{T}> {{
     files: List[List[str]] = []
     cur: List[str] = []
     for si in range(n_stages):
-        src, nscr = StageGen(spec, si, tag).generate()
+        src, nscr = stage_generator(spec, si, tag, mode).generate()
         scratch_counts[si] = nscr
         cur.append(src)
         if len(cur) >= stages_per_file:

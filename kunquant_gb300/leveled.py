@@ -1,0 +1,557 @@
+"""Leveled kernels: a time-series stage split into time-parallel and scan kernels.
+
+The reference walks every stage sequentially over time, one stock block per
+task (``KunQuant/passes/CodegenCpp.py:189``).  Most ops do not need that: a
+back-window loop's output at time t depends only on the window's values, and
+the order-statistic window of the skip-list ops is fully determined by the
+last W values.  Only the history-dependent states -- Kahan running sums
+(``FastWindowedSum``), the regression sums (``WindowedLinearRegression``) and
+``ExpMovingAvg`` -- need a sequential scan from the first row.
+
+Each op of a stage gets a *level*.  Even levels are time-parallel kernels (one
+thread per stock x time chunk, no carried state; order-statistic windows are
+rebuilt exactly with a W-row warm-up).  Odd levels are scan kernels: one thread
+per stock x state walks the whole time axis and stores the state's per-row
+result.  Values that cross levels are materialised in [T][S] scratch buffers;
+cheap pointwise ops are recomputed where they are needed.  A windowed read
+(loop, BackRef, skip list, running sum) only reads series materialised at an
+earlier level, so every kernel reads exactly the values the sequential
+reference computes and the arithmetic of every op is unchanged.
+"""
+from typing import Dict, List, Optional, Set, Tuple
+
+from . import contraction
+
+SEQ = {"FastWindowedSum", "WindowedLinearRegression", "ExpMovingAvg"}
+UNSUPPORTED = {"Accumulator", "SetAccumulator"}
+LR_CONS = {"WindowedLinearRegressionRSqaureImpl", "WindowedLinearRegressionSlopeImpl",
+           "WindowedLinearRegressionResiImpl"}
+SL_CONS = {"SkipListQuantile", "SkipListRank", "SkipListMin", "SkipListMax", "SkipListArgMin"}
+REDUCTIONS = {"ReduceAdd", "ReduceMul", "ReduceMin", "ReduceMax", "ReduceArgMax",
+              "ReduceArgMin", "ReduceRank", "ReduceDecayLinear"}
+ANCHORS = SEQ | LR_CONS | SL_CONS | REDUCTIONS | {"WindowedTempOutput", "Output", "SkipListState",
+                                                  "ForeachBackWindow"}
+
+
+def _even_ge(x: int) -> int:
+    x = max(x, 0)
+    return x if x % 2 == 0 else x + 1
+
+
+def _odd_ge(x: int) -> int:
+    x = max(x, 1)
+    return x if x % 2 == 1 else x + 1
+
+
+class Unsupported(Exception):
+    pass
+
+
+class StagePlan:
+    """Level assignment of one time-series stage."""
+
+    def __init__(self, ops: List[dict]):
+        self.ops = ops
+        n = len(ops)
+        for op in ops:
+            if op["k"] in UNSUPPORTED:
+                raise Unsupported(op["k"])
+            if op["k"] == "ForeachBackWindow" and op.get("p", -1) >= 0:
+                raise Unsupported("nested loop")
+        self.lv: List[int] = [-1] * n
+        self.loop_chain: Dict[int, List[int]] = {}
+        self._chains()
+        self._assign()
+
+    # loops merged by merge_loops share reductions: they form one chain
+    def _chains(self):
+        ops = self.ops
+        chain: List[int] = []
+        for i, op in enumerate(ops):
+            if op["k"] != "ForeachBackWindow":
+                continue
+            if op.get("copy_prev_body") and chain:
+                chain.append(i)
+            else:
+                chain = [i]
+            for j in chain:
+                self.loop_chain[j] = chain
+
+    def body(self, loop: int) -> List[int]:
+        return [j for j, o in enumerate(self.ops) if o.get("p", -1) == loop]
+
+    def windowed_source(self, i: int) -> Optional[int]:
+        op = self.ops[i]
+        k = op["k"]
+        if k in ("FastWindowedSum", "WindowedLinearRegression", "BackRef"):
+            return op["in"][0]
+        if k == "IterValue":
+            return op["in"][1]
+        if k == "SkipListState":
+            return self.ops[op["in"][0]]["in"][0]
+        return None
+
+    def _assign(self):
+        ops, lv = self.ops, self.lv
+        done_chain = set()
+        windowed_outputs = set()
+        for i, op in enumerate(ops):
+            ws = self.windowed_source(i)
+            if ws is not None and ops[ws]["k"] == "Output":
+                windowed_outputs.add(ws)
+        for i, op in enumerate(ops):
+            k = op["k"]
+            ins = op["in"]
+            if op.get("p", -1) >= 0:
+                continue
+            if k in ("Input", "ConstantOp"):
+                lv[i] = -1
+            elif k in ("FastWindowedSum", "WindowedLinearRegression"):
+                src = ins[0]
+                lv[i] = _odd_ge(lv[src] + 1 if lv[src] >= 0 else 0)
+            elif k == "ExpMovingAvg":
+                lv[i] = _odd_ge(max(lv[j] for j in ins))
+            elif k in LR_CONS:
+                lv[i] = lv[ins[0]]
+                if any(lv[j] > lv[i] for j in ins[1:]):
+                    raise Unsupported("regression residual of a later value")
+            elif k == "SkipListState":
+                src = self.windowed_source(i)
+                if ins[1] != src:
+                    raise Unsupported("skip list over a different current value")
+                lv[i] = _even_ge(lv[src] + 1 if lv[src] >= 0 else 0)
+            elif k in SL_CONS:
+                lv[i] = lv[ins[0]]
+                if any(lv[j] > lv[i] for j in ins[1:]):
+                    raise Unsupported("skip-list rank of a later value")
+            elif k == "WindowedTempOutput":
+                lv[i] = _even_ge(lv[ins[0]])
+            elif k == "ForeachBackWindow":
+                chain = self.loop_chain[i]
+                if chain[0] not in done_chain:
+                    base = 0
+                    for lp in chain:
+                        for j in self.body(lp):
+                            bo = ops[j]
+                            if bo["k"] == "IterValue":
+                                s = bo["in"][1]
+                                base = max(base, lv[s] + 1 if lv[s] >= 0 else 0)
+                            else:
+                                for x in bo["in"]:
+                                    if ops[x].get("p", -1) < 0 and ops[x]["k"] != "ForeachBackWindow":
+                                        base = max(base, lv[x])
+                    for j, q in enumerate(ops):
+                        if q["k"] == "ReduceRank" and contraction.reduction_loop(ops, j) in chain:
+                            base = max(base, lv[q["in"][1]])
+                    L = _even_ge(base)
+                    for lp in chain:
+                        lv[lp] = L
+                        for j in self.body(lp):
+                            lv[j] = L
+                    done_chain.add(chain[0])
+            elif k in REDUCTIONS:
+                lv[i] = lv[contraction.reduction_loop(ops, i)]
+            elif k == "BackRef":
+                src = ins[0]
+                lv[i] = lv[src] + 1 if lv[src] >= 0 else -1
+            elif k == "Output":
+                lv[i] = _even_ge(lv[ins[0]]) if i in windowed_outputs else None
+            else:
+                lv[i] = max([self._vl(j) for j in ins] + [-1])
+        # outputs not read back in the stage go to the last parallel level
+        top = max([x for x in lv if x is not None] + [0])
+        final = _even_ge(top)
+        for i, op in enumerate(ops):
+            if op["k"] == "Output" and lv[i] is None:
+                lv[i] = final
+        self.final = final
+        self.levels = sorted({lv[i] for i, op in enumerate(ops)
+                              if op["k"] in ANCHORS and op.get("p", -1) < 0 and lv[i] >= 0})
+        if not self.levels:
+            self.levels = [0]
+
+    def _vl(self, j: int) -> int:
+        while self.lv[j] is None:
+            j = self.ops[j]["in"][0]
+        return self.lv[j]
+
+    def is_anchor(self, i: int) -> bool:
+        return self.ops[i]["k"] in ANCHORS and self.ops[i].get("p", -1) < 0
+
+    def is_source(self, i: int) -> bool:
+        return self.ops[i]["k"] in ("Input", "ConstantOp")
+
+    # ---------------------------------------------------------------- sets
+    def chain_members(self, loop: int) -> List[int]:
+        """All ops of the loop chain of `loop`: loops, body ops, reductions."""
+        ops = self.ops
+        chain = self.loop_chain[loop]
+        out = list(chain)
+        for lp in chain:
+            out += self.body(lp)
+        for j, q in enumerate(ops):
+            if q["k"] in REDUCTIONS and contraction.reduction_loop(ops, j) in chain:
+                out.append(j)
+        return out
+
+    def value_source(self, j: int, level: int) -> int:
+        """Outputs and windowed temps are copies of their input; when they are
+        materialised later than `level`, their input is used instead."""
+        ops = self.ops
+        while ops[j]["k"] in ("Output", "WindowedTempOutput") and self.lv[j] > level:
+            j = ops[j]["in"][0]
+        return j
+
+    def closure(self, roots: List[int], level: int) -> Tuple[Set[int], Set[int], Set[int]]:
+        """(ops computed at `level` for `roots`, ops whose value is read from
+        memory, series read through windows)."""
+        ops, lv = self.ops, self.lv
+        comp: Set[int] = set()
+        vreads: Set[int] = set()
+        wreads: Set[int] = set()
+        stack = list(roots)
+        while stack:
+            i = stack.pop()
+            if i in comp:
+                continue
+            op = ops[i]
+            k = op["k"]
+            if k == "Input":
+                vreads.add(i)
+                continue
+            if self.is_anchor(i) and k != "ForeachBackWindow" and op.get("p", -1) < 0 and lv[i] < level:
+                vreads.add(i)
+                continue
+            if self.is_anchor(i) and op.get("p", -1) < 0 and lv[i] > level:
+                raise Unsupported(f"op {i} ({k}) of level {lv[i]} needed at level {level}")
+            comp.add(i)
+            loop = None
+            if k == "ForeachBackWindow":
+                loop = i
+            elif k in REDUCTIONS:
+                loop = contraction.reduction_loop(ops, i)
+            elif op.get("p", -1) >= 0:
+                loop = op["p"]
+            if loop is not None:
+                for j in self.chain_members(loop):
+                    if j not in comp:
+                        stack.append(j)
+            deps: List[int] = []
+            if k == "IterValue":
+                wreads.add(op["in"][1])
+            elif k == "ForeachBackWindow":
+                pass
+            elif k in REDUCTIONS:
+                deps = op["in"][1:]
+            elif k == "BackRef":
+                wreads.add(op["in"][0])
+            elif k in ("FastWindowedSum", "WindowedLinearRegression"):
+                wreads.add(op["in"][0])
+                deps = [op["in"][0]]
+            elif k == "SkipListState":
+                wreads.add(self.windowed_source(i))
+                deps = list(op["in"])
+            else:
+                deps = list(op["in"])
+            for d in deps:
+                if ops[d].get("p", -1) >= 0 and op.get("p", -1) < 0:
+                    continue
+                stack.append(self.value_source(d, level) if ops[d].get("p", -1) < 0 else d)
+        return comp, vreads, wreads
+
+
+# ====================================================================== codegen
+from .codegen import StageGen  # noqa: E402
+
+PAR_CHUNK = 32
+
+
+class LeveledGen(StageGen):
+    """Emits the leveled kernels of one time-series stage."""
+
+    def __init__(self, spec: dict, si: int, tag: str):
+        super().__init__(spec, si, tag)
+        self.plan = StagePlan(self.ops)
+        self.fplan = contraction.plan(self.ops)
+        self.cur_level = None
+        self.cur_comp: Set[int] = set()
+
+    def val(self, i: int) -> str:
+        if self.cur_level is not None and self.ops[i].get("p", -1) < 0:
+            i = self.plan.value_source(i, self.cur_level)
+        if self.ops[i]["k"] in REDUCTIONS and i not in self.cur_comp:
+            return f"v{i}"  # materialised at an earlier level, loaded per row
+        return super().val(i)
+
+    # ------------------------------------------------------------------ memory
+    def _kernels(self):
+        plan, ops, lv = self.plan, self.ops, self.plan.lv
+        ks = []
+        for L in plan.levels:
+            if L % 2 == 0:
+                roots = [i for i in range(len(ops)) if plan.is_anchor(i) and lv[i] == L
+                         and ops[i]["k"] not in SEQ]
+                comp, vr, wr = plan.closure(roots, L)
+                ks.append({"level": L, "kind": "par", "roots": roots, "comp": comp, "vr": vr, "wr": wr})
+            else:
+                roles = []
+                for i in range(len(ops)):
+                    if ops[i]["k"] in SEQ and lv[i] == L:
+                        roots = [i] + [j for j, q in enumerate(ops) if q["k"] in LR_CONS and q["in"][0] == i]
+                        comp, vr, wr = plan.closure(roots, L)
+                        roles.append({"roots": roots, "comp": comp, "vr": vr, "wr": wr})
+                if roles:
+                    ks.append({"level": L, "kind": "scan", "roles": roles})
+        return ks
+
+    def _mem_ptr(self, j: int, decl: List[str], seen: Set[int]):
+        """Pointer b{j} + stride st{j} of op j's [T][S] series."""
+        if j in seen:
+            return
+        seen.add(j)
+        op = self.ops[j]
+        T = self.T
+        k = op["k"]
+        if k in ("Input", "Output"):
+            sl = self.slot(op["buf"])
+            const = "const " if k == "Input" else ""
+            lay = self.layout_of(op)
+            user = self.is_user_input(op)
+            rowoff = "start" if user else "0"
+            rows = "total_time" if user else "length"
+            if op.get("single_value"):
+                decl.append(f"  {const}{T}* __restrict__ b{j} = ({const}{T}*)P.p[{sl}] + s;")
+                decl.append(f"  const long long st{j} = 0;")
+            elif lay == "TS":
+                decl.append(f"  {const}{T}* __restrict__ b{j} = ({const}{T}*)P.p[{sl}] + {rowoff} * S + s;")
+                decl.append(f"  const long long st{j} = S;")
+            else:
+                L = self.blocking
+                decl.append(f"  {const}{T}* __restrict__ b{j} = ({const}{T}*)P.p[{sl}] + "
+                            f"(s / {L}) * {rows} * {L} + {rowoff} * {L} + s % {L};")
+                decl.append(f"  const long long st{j} = {L};")
+        else:
+            sc = self.scratch[j]
+            decl.append(f"  {T}* __restrict__ b{j} = ({T}*)P.w[{sc}] + s;")
+            decl.append(f"  const long long st{j} = S;")
+
+    # ------------------------------------------------------------------ ops
+    def emit_top(self, i: int, ind: str, loops: Dict, comp: Set[int]):
+        ops, T = self.ops, self.T
+        op = ops[i]
+        k = op["k"]
+        a = op["in"]
+        fplan = self.fplan
+        if k == "Input":
+            return  # loaded at the top of the iteration
+        if k in ("Output", "WindowedTempOutput"):
+            self.lines.append(f"{ind}b{i}[t * st{i}] = {self.val(a[0])};")
+            self.lines.append(f"{ind}const {T} v{i} = {self.val(a[0])};")
+        elif k == "ForeachBackWindow":
+            body, reds, own = loops[i]
+            w, seg = op["window"], op.get("segment_end", 0)
+            for r in own:
+                self.lines.append(f"{ind}{self.reduction_decl(r)}")
+            self.lines.append(f"{ind}for (int iter = {w - 1}; iter >= {seg}; --iter) {{")
+            bind = ind + "  "
+            for j in body:
+                bo = ops[j]
+                if bo["k"] == "IterValue":
+                    self.lines.append(f"{bind}const {T} v{j} = {self.window_read(bo['in'][1], 'iter')};")
+                elif bo["k"] == "WindowLoopIndex":
+                    self.lines.append(f"{bind}const {T} v{j} = ({T})({bo.get('loop_window', w)} - 1 - iter);")
+                elif not self.emit_simple(j, bind, fplan):
+                    raise Unsupported(f"op in loop body: {bo['k']}")
+            for r in reds:
+                self.reduction_step(r, fplan, bind)
+            self.lines.append(f"{ind}}}")
+        elif k in REDUCTIONS:
+            pass
+        elif k == "BackRef":
+            self.lines.append(f"{ind}const {T} v{i} = {self.window_read(a[0], op['window'])};")
+        elif k == "FastWindowedSum":
+            self.lines.append(f"{ind}const {T} v{i} = fw{i}.step({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
+        elif k == "WindowedLinearRegression":
+            shared = "true" if contraction.regression_shares_square(ops, i) else "false"
+            self.lines.append(f"{ind}lr{i}.template step<{shared}>({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
+        elif k == "WindowedLinearRegressionRSqaureImpl":
+            self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.rsq();")
+        elif k == "WindowedLinearRegressionSlopeImpl":
+            self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.slope();")
+        elif k == "WindowedLinearRegressionResiImpl":
+            self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.resi({self.val(a[1])});")
+        elif k == "ExpMovingAvg":
+            self.lines.append(f"{ind}const {T} v{i} = ema{i}.step({self.val(a[0])});")
+        elif k == "SkipListState":
+            self.lines.append(f"{ind}sl{i}.step({self.val(a[0])}, {self.val(a[1])}, (int)t);")
+        elif k == "SkipListQuantile":
+            self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.quantile<{T}>({self.lit(op['q'])});")
+        elif k == "SkipListMin":
+            self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.vmin<{T}>();")
+        elif k == "SkipListMax":
+            self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.vmax<{T}>();")
+        elif k == "SkipListArgMin":
+            self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.argmin<{T}>(t);")
+        elif k == "SkipListRank":
+            self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.rank<{T}>({self.val(a[1])});")
+        elif not self.emit_simple(i, ind, fplan):
+            raise Unsupported(f"op {k}")
+
+    def _loops(self):
+        ops = self.ops
+        loops = {}
+        prev = None
+        n = len(ops)
+        for i, op in enumerate(ops):
+            if op["k"] != "ForeachBackWindow":
+                continue
+            body, reds = [], []
+            if op.get("copy_prev_body") and prev is not None:
+                body += loops[prev][0]
+                reds += loops[prev][1]
+            own = [j for j in range(n) if ops[j]["k"] in REDUCTIONS
+                   and contraction.reduction_loop(ops, j) == i]
+            body += [j for j in range(n) if ops[j].get("p", -1) == i]
+            reds += own
+            loops[i] = (body, reds, own)
+            prev = i
+        return loops
+
+    def _state_decl(self, i: int) -> Optional[str]:
+        op, T = self.ops[i], self.T
+        k = op["k"]
+        if k == "FastWindowedSum":
+            return f"kun::FWSum<{T}> fw{i}({op['window']});"
+        if k == "WindowedLinearRegression":
+            return f"kun::LinReg<{T}, {op['window']}> lr{i};"
+        if k == "ExpMovingAvg":
+            init = f"kun::knan<{T}>()"
+            if len(op["in"]) == 2:
+                init = f"b{op['in'][1]}[0]"
+            return f"kun::EMA<{T}, {op['window']}> ema{i}({init});"
+        if k == "SkipListState":
+            return f"kun::SortedWindow<{op['window']}> sl{i};"
+        return None
+
+    def _body(self, comp: Set[int], vr: Set[int], stores: List[int], loops, ind: str):
+        ops, T = self.ops, self.T
+        self.cur_comp = comp
+        for j in sorted(vr):
+            if ops[j]["k"] == "Input" and ops[j].get("single_value"):
+                self.lines.append(f"{ind}const {T} v{j} = b{j}[0];")
+            else:
+                self.lines.append(f"{ind}const {T} v{j} = b{j}[t * st{j}];")
+        for i in range(len(ops)):
+            if i in comp and ops[i].get("p", -1) < 0:
+                self.emit_top(i, ind, loops, comp)
+        for i in stores:
+            self.lines.append(f"{ind}b{i}[t * st{i}] = {self.val(i)};")
+
+    # ------------------------------------------------------------------ stage
+    def gen_ts(self):
+        ops, T = self.ops, self.T
+        ks = self._kernels()
+        loops = self._loops()
+        # series read by a later kernel need a memory home
+        for i, op in enumerate(ops):
+            if op["k"] == "WindowedTempOutput" and op.get("p", -1) < 0:
+                self.scratch[i] = len(self.scratch)
+        reads = set()
+        for kd in ks:
+            groups = kd["roles"] if kd["kind"] == "scan" else [kd]
+            for g in groups:
+                reads |= g["vr"] | g["wr"]
+        mats = sorted(j for j in reads if ops[j]["k"] not in ("Input", "Output", "WindowedTempOutput"))
+        for j in mats:
+            self.scratch[j] = len(self.scratch)
+        srcs, calls = [], []
+        for kd in ks:
+            L = kd["level"]
+            kname = f"{self.kname}_L{L}"
+            decl: List[str] = []
+            seen: Set[int] = set()
+            self.lines = []
+            self.cur_level = L
+            if kd["kind"] == "par":
+                comp, vr, wr = kd["comp"], kd["vr"], kd["wr"]
+                for j in sorted(vr | wr | {i for i in comp if ops[i]["k"] in ("Output", "WindowedTempOutput")}
+                                | {i for i in comp if i in self.scratch}):
+                    self._mem_ptr(j, decl, seen)
+                for i in sorted(comp):
+                    if ops[i]["k"] == "ExpMovingAvg" and len(ops[i]["in"]) == 2:
+                        self._mem_ptr(ops[i]["in"][1], decl, seen)
+                stores = [i for i in sorted(comp) if i in mats]
+                sls = [i for i in sorted(comp) if ops[i]["k"] == "SkipListState"]
+                states = [self._state_decl(i) for i in sls]
+                wmax = max([ops[i]["window"] for i in sls] + [0])
+                chunk = max(PAR_CHUNK, 4 * wmax)
+                self.lines.append(f"  const long long t0 = (long long)blockIdx.y * {chunk};")
+                self.lines.append(f"  const long long t1 = t0 + {chunk} < length ? t0 + {chunk} : length;")
+                for sd in states:
+                    self.lines.append(f"  {sd}")
+                if sls:
+                    # rebuild the order-statistic windows from the previous rows;
+                    # only values inserted in this warm-up are removed
+                    self.lines.append(f"  const long long tw = t0 > {wmax} ? t0 - {wmax} : 0;")
+                    self.lines.append("  for (long long t = tw; t < t0; ++t) {")
+                    for i in sls:
+                        src = self.plan.windowed_source(i)
+                        W = ops[i]["window"]
+                        self.lines.append(f"    sl{i}.step((t - {W} >= tw) ? {self.read_at(src, f't - {W}')} : kun::knan<{T}>(), "
+                                          f"{self.read_at(src, 't')}, (int)t);")
+                    self.lines.append("  }")
+                self.lines.append("  for (long long t = t0; t < t1; ++t) {")
+                self._body(comp, vr, stores, loops, "    ")
+                self.lines.append("  }")
+                grid_y = f"(unsigned)((a->length + {chunk} - 1) / {chunk})"
+            else:
+                roles = kd["roles"]
+                allr = set()
+                for r in roles:
+                    allr |= r["vr"] | r["wr"] | {i for i in r["roots"] if i in self.scratch}
+                    for i in r["comp"]:
+                        if ops[i]["k"] == "ExpMovingAvg" and len(ops[i]["in"]) == 2:
+                            allr.add(ops[i]["in"][1])
+                for j in sorted(allr):
+                    self._mem_ptr(j, decl, seen)
+                self.lines.append("  switch (blockIdx.y) {")
+                for ri, r in enumerate(roles):
+                    self.lines.append(f"  case {ri}: {{")
+                    for i in sorted(r["comp"]):
+                        sd = self._state_decl(i)
+                        if sd:
+                            self.lines.append(f"    {sd}")
+                    self.lines.append("    for (long long t = 0; t < length; ++t) {")
+                    stores = [i for i in r["roots"] if i in mats]
+                    self._body(r["comp"], r["vr"], stores, loops, "      ")
+                    self.lines.append("    }")
+                    self.lines.append("  } break;")
+                self.lines.append("  default: break;")
+                self.lines.append("  }")
+                grid_y = str(len(roles))
+            srcs.append(f"""
+__global__ void __launch_bounds__(KUN_TS_THREADS) {kname}(const P_{self.kname} P) {{
+  const long long S = P.S;
+  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= S) return;
+  const long long total_time = P.total_time, start = P.start, length = P.length;
+  (void)total_time; (void)start;
+{chr(10).join(decl)}
+{chr(10).join(self.lines)}
+}}
+""")
+            calls.append(f"  {kname}<<<dim3((unsigned)((a->num_stocks + KUN_TS_THREADS - 1) / KUN_TS_THREADS), "
+                         f"{grid_y}), KUN_TS_THREADS, 0, (cudaStream_t)stream>>>(P);\n"
+                         f"  if (cudaError_t e = cudaGetLastError()) return (int)e;")
+        nslots = max(1, len(self.slots))
+        nscr = max(1, len(self.scratch))
+        pstruct = f"P_{self.kname}"
+        head = f"""
+struct {pstruct} {{
+  void* p[{nslots}];
+  void* w[{nscr}];
+  long long S, total_time, start, length;
+}};
+"""
+        launch = self.launcher(pstruct, "\n".join(calls))
+        return head + "".join(srcs), launch
