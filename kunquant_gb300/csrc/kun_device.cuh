@@ -372,4 +372,82 @@ template <int W> struct SortedWindow {
     }
 };
 
+// Register-resident form of the order-statistic window for W <= 64: the
+// window is a sorted array of W registers, empty slots hold NaN (they never
+// compare true, so they stay at the end and drop out of every count).  Every
+// update is a fixed, branch-free compare/select network over the W slots, so
+// all stocks of a warp execute the same instructions.  Semantics are those of
+// SortedWindow above: removal takes the first equal value, insertion goes
+// after equal values.
+template <typename T, int W, bool IDX> struct RegWindow {
+    T v[W];
+    int ix[IDX ? W : 1];
+    int size = 0;
+    int last_rank = 0;
+    __device__ __forceinline__ RegWindow() {
+#pragma unroll
+        for (int j = 0; j < W; j++) v[j] = knan<T>();
+    }
+    // x must be present (the caller removes only values it inserted)
+    __device__ __forceinline__ void remove(T x) {
+        int p = 0;
+#pragma unroll
+        for (int j = 0; j < W; j++) p += (v[j] < x) ? 1 : 0;
+#pragma unroll
+        for (int j = 0; j < W - 1; j++) {
+            const bool sh = j >= p;
+            v[j] = sh ? v[j + 1] : v[j];
+            if (IDX) ix[j] = sh ? ix[j + 1] : ix[j];
+        }
+        v[W - 1] = knan<T>();
+        size--;
+    }
+    __device__ __forceinline__ int insert(T y, int index) {
+        int q = 0;
+#pragma unroll
+        for (int j = 0; j < W; j++) q += (v[j] <= y) ? 1 : 0;
+#pragma unroll
+        for (int j = W - 1; j > 0; j--) {
+            v[j] = (j > q) ? v[j - 1] : ((j == q) ? y : v[j]);
+            if (IDX) ix[j] = (j > q) ? ix[j - 1] : ((j == q) ? index : ix[j]);
+        }
+        v[0] = (q == 0) ? y : v[0];
+        if (IDX) ix[0] = (q == 0) ? index : ix[0];
+        size++;
+        return q;
+    }
+    __device__ __forceinline__ int min_rank(T x) const {
+        int p = 0;
+#pragma unroll
+        for (int j = 0; j < W; j++) p += (v[j] < x) ? 1 : 0;
+        return p;
+    }
+    __device__ __forceinline__ void step(T oldv, T newv, int index) {
+        if (!kisnan(oldv)) remove(oldv);
+        if (!kisnan(newv)) last_rank = insert(newv, index);
+    }
+    // quantile with the rank arithmetic done at compile time: ID =
+    // int(q * (W - 1)) and frac = q * (W - 1) - ID in the module dtype
+    template <int ID, bool EXACT> __device__ __forceinline__ T quantile(T frac) const {
+        if (size != W) return knan<T>();
+        if (EXACT) return v[ID];
+        double lo = (double)v[ID], hi = (double)v[ID + 1];
+        return (T)__fma_rn(__dsub_rn(hi, lo), (double)frac, lo);
+    }
+    __device__ __forceinline__ T vmin() const { return size != W ? knan<T>() : v[0]; }
+    __device__ __forceinline__ T vmax() const { return size != W ? knan<T>() : v[W - 1]; }
+    __device__ __forceinline__ T argmin(long long cur_idx) const {
+        if (size != W) return knan<T>();
+        return (T)(unsigned long long)((unsigned long long)ix[0] + (unsigned long long)size -
+                                       (unsigned long long)cur_idx);
+    }
+    __device__ __forceinline__ T rank(T cur) const {
+        if (size != W) return knan<T>();
+        double r = last_rank + 1;
+        double rmin = min_rank(cur) + 1;
+        r = (((r * (r + 1) / 2) - ((rmin - 1) * rmin / 2)) / (r - rmin + 1));
+        return (T)r;
+    }
+};
+
 }  // namespace kun

@@ -264,6 +264,7 @@ class StagePlan:
 from .codegen import StageGen  # noqa: E402
 
 PAR_CHUNK = 32
+REG_WINDOW_MAX = 64
 
 
 class LeveledGen(StageGen):
@@ -291,8 +292,8 @@ class LeveledGen(StageGen):
             if L % 2 == 0:
                 roots = [i for i in range(len(ops)) if plan.is_anchor(i) and lv[i] == L
                          and ops[i]["k"] not in SEQ]
-                comp, vr, wr = plan.closure(roots, L)
-                ks.append({"level": L, "kind": "par", "roots": roots, "comp": comp, "vr": vr, "wr": wr})
+                for role in self._par_roles(roots, L):
+                    ks.append(dict(role, level=L, kind="par"))
             else:
                 roles = []
                 for i in range(len(ops)):
@@ -303,6 +304,51 @@ class LeveledGen(StageGen):
                 if roles:
                     ks.append({"level": L, "kind": "scan", "roles": roles})
         return ks
+
+    def _weight(self, comp: Set[int]) -> float:
+        ops = self.ops
+        w = 0.0
+        for i in comp:
+            k = ops[i]["k"]
+            if k == "ForeachBackWindow":
+                w += (ops[i]["window"] - ops[i].get("segment_end", 0)) * 4
+            elif k == "SkipListState":
+                w += ops[i]["window"] * 12
+        return w
+
+    def _par_roles(self, roots: List[int], L: int) -> List[dict]:
+        """Independent parts of a parallel level (no shared computed op) run as
+        separate kernels: each gets its own registers and time chunking.  Cheap
+        pointwise parts are kept together."""
+        plan = self.plan
+        closures = []
+        for r in roots:
+            comp, vr, wr = plan.closure([r], L)
+            closures.append(([r], comp, vr, wr))
+        # union components that share computed ops (not constants)
+        groups: List[list] = []
+        for c in closures:
+            merged = [c]
+            rest = []
+            for g in groups:
+                gcomp = set().union(*[x[1] for x in g])
+                shared = {i for i in (gcomp & c[1]) if self.ops[i]["k"] != "ConstantOp"}
+                if shared:
+                    merged += g
+                else:
+                    rest.append(g)
+            groups = rest + [merged]
+        heavy, light = [], []
+        for g in groups:
+            comp = set().union(*[x[1] for x in g])
+            (heavy if self._weight(comp) >= 40 else light).append(g)
+        parts = heavy + ([sum(light, [])] if light else [])
+        out = []
+        for g in parts:
+            rts = sorted(sum([x[0] for x in g], []))
+            comp, vr, wr = plan.closure(rts, L)
+            out.append({"roots": rts, "comp": comp, "vr": vr, "wr": wr})
+        return out
 
     def _mem_ptr(self, j: int, decl: List[str], seen: Set[int]):
         """Pointer b{j} + stride st{j} of op j's [T][S] series."""
@@ -384,6 +430,17 @@ class LeveledGen(StageGen):
             self.lines.append(f"{ind}const {T} v{i} = ema{i}.step({self.val(a[0])});")
         elif k == "SkipListState":
             self.lines.append(f"{ind}sl{i}.step({self.val(a[0])}, {self.val(a[1])}, (int)t);")
+        elif k in SL_CONS and self._reg_window(a[0]):
+            if k == "SkipListQuantile":
+                self.lines.append(f"{ind}const {T} v{i} = {self._quantile(i)};")
+            elif k == "SkipListMin":
+                self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.vmin();")
+            elif k == "SkipListMax":
+                self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.vmax();")
+            elif k == "SkipListArgMin":
+                self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.argmin(t);")
+            else:
+                self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.rank({self.val(a[1])});")
         elif k == "SkipListQuantile":
             self.lines.append(f"{ind}const {T} v{i} = sl{a[0]}.quantile<{T}>({self.lit(op['q'])});")
         elif k == "SkipListMin":
@@ -430,8 +487,39 @@ class LeveledGen(StageGen):
                 init = f"b{op['in'][1]}[0]"
             return f"kun::EMA<{T}, {op['window']}> ema{i}({init});"
         if k == "SkipListState":
+            if self._reg_window(i):
+                idx = "true" if any(q["k"] == "SkipListArgMin" and q["in"][0] == i for q in self.ops) else "false"
+                return f"kun::RegWindow<{T}, {op['window']}, {idx}> sl{i};"
             return f"kun::SortedWindow<{op['window']}> sl{i};"
         return None
+
+    def _reg_window(self, i: int) -> bool:
+        return self.ops[i]["window"] <= REG_WINDOW_MAX
+
+    def _quantile(self, i: int) -> str:
+        """SkipListQuantile with idx = int(q*(W-1)) and its fraction folded at
+        generation time in the module dtype (Quantile.hpp:94-101)."""
+        import numpy as np
+        from .codegen import _f32_exact
+        from fractions import Fraction
+        op = self.ops[i]
+        st = op["in"][0]
+        W = self.ops[st]["window"]
+        if self.dtype == "float":
+            q = np.float32(_f32_exact(op["q"]))
+            iwf = np.float32(q * np.float32(W - 1))
+            idx = int(iwf)
+            exact = np.float32(idx) == iwf
+            frac = np.float32(iwf - np.float32(idx))
+        else:
+            q = float(Fraction(op["q"]))
+            iwf = q * float(W - 1)
+            idx = int(iwf)
+            exact = float(idx) == iwf
+            frac = iwf - float(idx)
+        if exact:
+            return f"sl{st}.template quantile<{idx}, true>(({self.T})0)"
+        return f"sl{st}.template quantile<{idx}, false>({self.lit(repr(float(frac)))})"
 
     def _body(self, comp: Set[int], vr: Set[int], stores: List[int], loops, ind: str):
         ops, T = self.ops, self.T
@@ -465,9 +553,9 @@ class LeveledGen(StageGen):
         for j in mats:
             self.scratch[j] = len(self.scratch)
         srcs, calls = [], []
-        for kd in ks:
+        for ki, kd in enumerate(ks):
             L = kd["level"]
-            kname = f"{self.kname}_L{L}"
+            kname = f"{self.kname}_L{L}_{ki}"
             decl: List[str] = []
             seen: Set[int] = set()
             self.lines = []
