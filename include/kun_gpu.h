@@ -117,15 +117,22 @@ void kunDestoryStream(KunStreamContextHandle context);
 KunStatus kunRunGraphEx(KunExecutorHandle exec, KunModuleHandle m, KunBufferNameMapHandle buffers,
                         size_t num_stocks, size_t total_time, size_t cur_time, size_t length,
                         int synchronize);
-/* Make the executor enqueue on an existing CUDA stream (cudaStream_t), e.g.
- * the caller's current stream; NULL restores the executor's own stream. */
+/* Order the executor's work after and before the caller's CUDA stream
+ * (cudaStream_t; 0 is the legacy default stream): runs start when the work
+ * already queued on that stream is done, and later work on that stream waits
+ * for the run.  The executor still computes on its own streams. */
 KunStatus kunExecutorSetStream(KunExecutorHandle exec, void *cuda_stream);
+/* Stop ordering with the caller's stream. */
+KunStatus kunExecutorClearStream(KunExecutorHandle exec);
 KunStatus kunExecutorSynchronize(KunExecutorHandle exec);
 /* Record a CUDA event after every stage launch of the following runs (1) or
  * stop (0); kunExecutorStageTimes returns the per-stage milliseconds of the
  * last run (stage ids in launch order), or -1 when profiling is off. */
 KunStatus kunExecutorSetProfiling(KunExecutorHandle exec, int enable);
 int kunExecutorStageTimes(KunExecutorHandle exec, int32_t *stage_ids, float *ms, int cap);
+/* Replay repeated runs (same module, shape and buffers) from a captured CUDA
+ * graph (1, the default) or always enqueue kernel by kernel (0). */
+KunStatus kunExecutorSetGraphs(KunExecutorHandle exec, int enable);
 /* Count of kernel launches of the last run (for instrumentation). */
 int64_t kunExecutorLastLaunchCount(KunExecutorHandle exec);
 /* Text of the last error of the calling thread ("" if none). */

@@ -135,64 +135,60 @@ class StageGen:
         return literal(text, self.dtype)
 
     # ------------------------------------------------------------ ops
-    def emit_simple(self, i: int, ind: str, fplan) -> bool:
+    def simple_expr(self, i: int, fplan):
+        """Right-hand side of a pointwise op, or None for other ops."""
         op = self.ops[i]
         k = op["k"]
         T = self.T
         a = op["in"]
-        out = f"{ind}const {T} v{i} = "
         if i in fplan:
             pos, prod = fplan[i]
             po = self.ops[prod]
             A = self.val(po["in"][0])
             B = self.val(po["in"][1]) if po["k"] == "Mul" else self.lit(po["value"])
             if k == "Add":
+                return f"kun::kfma({A}, {B}, {self.val(a[1 - pos])})"
+            if k == "Sub":
                 o = self.val(a[1 - pos])
-                self.lines.append(f"{out}kun::kfma({A}, {B}, {o});")
-            elif k == "Sub":
-                o = self.val(a[1 - pos])
-                if pos == 0:
-                    self.lines.append(f"{out}kun::kfma({A}, {B}, -({o}));")
-                else:
-                    self.lines.append(f"{out}kun::kfma(-({A}), {B}, {o});")
-            elif k == "AddConst":
-                self.lines.append(f"{out}kun::kfma({A}, {B}, {self.lit(op['value'])});")
-            elif k == "SubConst":
+                return f"kun::kfma({A}, {B}, -({o}))" if pos == 0 else f"kun::kfma(-({A}), {B}, {o})"
+            if k == "AddConst":
+                return f"kun::kfma({A}, {B}, {self.lit(op['value'])})"
+            if k == "SubConst":
                 c = self.lit(op["value"])
-                if op.get("swap"):
-                    self.lines.append(f"{out}kun::kfma(-({A}), {B}, {c});")
-                else:
-                    self.lines.append(f"{out}kun::kfma({A}, {B}, -({c}));")
-            else:
-                raise RuntimeError("bad fused op " + k)
-            return True
+                return f"kun::kfma(-({A}), {B}, {c})" if op.get("swap") else f"kun::kfma({A}, {B}, -({c}))"
+            raise RuntimeError("bad fused op " + k)
         if k == "ConstantOp":
-            self.lines.append(f"{out}{self.lit(op['value'])};")
-        elif k in ELEMENTWISE_BIN:
-            self.lines.append(f"{out}kun::{ELEMENTWISE_BIN[k]}({self.val(a[0])}, {self.val(a[1])});")
-        elif k in CMP:
-            self.lines.append(f"{out}kun::kmask<{T}>({self.val(a[0])} {CMP[k]} {self.val(a[1])});")
-        elif k in CONST_BIN:
+            return self.lit(op["value"])
+        if k in ELEMENTWISE_BIN:
+            return f"kun::{ELEMENTWISE_BIN[k]}({self.val(a[0])}, {self.val(a[1])})"
+        if k in CMP:
+            return f"kun::kmask<{T}>({self.val(a[0])} {CMP[k]} {self.val(a[1])})"
+        if k in CONST_BIN:
             c = self.lit(op["value"])
             x, y = (c, self.val(a[0])) if op.get("swap") else (self.val(a[0]), c)
-            self.lines.append(f"{out}kun::{CONST_BIN[k]}({x}, {y});")
-        elif k in CONST_CMP:
+            return f"kun::{CONST_BIN[k]}({x}, {y})"
+        if k in CONST_CMP:
             c = self.lit(op["value"])
             x, y = (c, self.val(a[0])) if op.get("swap") else (self.val(a[0]), c)
-            self.lines.append(f"{out}kun::kmask<{T}>({x} {CONST_CMP[k]} {y});")
-        elif k in UNARY:
-            self.lines.append(f"{out}kun::{UNARY[k]}({self.val(a[0])});")
-        elif k == "Log":
+            return f"kun::kmask<{T}>({x} {CONST_CMP[k]} {y})"
+        if k in UNARY:
+            return f"kun::{UNARY[k]}({self.val(a[0])})"
+        if k == "Log":
             fn = "klogfast" if self.spec.get("options", {}).get("fast_log", True) else "klogstd"
-            self.lines.append(f"{out}kun::{fn}({self.val(a[0])});")
-        elif k == "SetInfOrNanToValue":
-            self.lines.append(f"{out}kun::ksetinfnan({self.val(a[0])}, {self.lit(op['value'])});")
-        elif k == "Select":
-            self.lines.append(f"{out}kun::kselect({self.val(a[0])}, {self.val(a[1])}, {self.val(a[2])});")
-        elif k == "ReturnFirstValue":
-            self.lines.append(f"{out}{self.val(a[0])};")
-        else:
+            return f"kun::{fn}({self.val(a[0])})"
+        if k == "SetInfOrNanToValue":
+            return f"kun::ksetinfnan({self.val(a[0])}, {self.lit(op['value'])})"
+        if k == "Select":
+            return f"kun::kselect({self.val(a[0])}, {self.val(a[1])}, {self.val(a[2])})"
+        if k == "ReturnFirstValue":
+            return self.val(a[0])
+        return None
+
+    def emit_simple(self, i: int, ind: str, fplan) -> bool:
+        e = self.simple_expr(i, fplan)
+        if e is None:
             return False
+        self.lines.append(f"{ind}const {self.T} v{i} = {e};")
         return True
 
     def reduction_decl(self, r: int) -> str:
@@ -469,12 +465,12 @@ extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
 """
         return src, launch
 
-    def generate(self) -> Tuple[str, int]:
+    def generate(self) -> Tuple[str, int, int]:
         if self.st["kind"] == "ts":
             src, launch = self.gen_ts()
         else:
             src, launch = self.gen_xsec()
-        return src + launch, len(self.scratch)
+        return src + launch, len(self.scratch), max(1, launch.count("<<<"))
 
 
 def stage_generator(spec: dict, si: int, tag: str, mode: str = "leveled") -> StageGen:
@@ -526,11 +522,13 @@ template <> struct LogTables<{T}> {{
     paths = []
     n_stages = len(spec["stages"])
     scratch_counts = [0] * n_stages
+    kernel_counts = [1] * n_stages
     files: List[List[str]] = []
     cur: List[str] = []
     for si in range(n_stages):
-        src, nscr = stage_generator(spec, si, tag, mode).generate()
+        src, nscr, nk = stage_generator(spec, si, tag, mode).generate()
         scratch_counts[si] = nscr
+        kernel_counts[si] = nk
         cur.append(src)
         if len(cur) >= stages_per_file:
             files.append(cur)
@@ -557,7 +555,7 @@ template <> struct LogTables<{T}> {{
     for si, st in enumerate(spec["stages"]):
         lines.append(f"  {{{_c_str(st['name'][:200])}, {kinds[st['kind']]}, {len(st['in'])}, st{si}_in, "
                      f"{len(st['out'])}, st{si}_out, {len(st.get('deps', []))}, st{si}_deps, "
-                     f"{st.get('pending', 0)}, {scratch_counts[si]}, 0, kst_{tag}_{si}_launch}},")
+                     f"{st.get('pending', 0)}, {scratch_counts[si]}, 0, kst_{tag}_{si}_launch, {kernel_counts[si]}}},")
     lines.append("};")
     bk = {"INPUT": "KUN_BUF_INPUT", "OUTPUT": "KUN_BUF_OUTPUT", "TEMP": "KUN_BUF_TEMP"}
     lines.append(f"static const KunGpuBufferDesc buffers_{tag}[] = {{")

@@ -202,7 +202,9 @@ template <typename T, bool IsMax> struct RArg {
 };
 template <typename T> struct RRank {
     T v, less = 0, eq = 0;
+    __device__ __forceinline__ RRank() {}
     __device__ __forceinline__ explicit RRank(T cur) : v(cur) {}
+    __device__ __forceinline__ void reset(T cur) { v = cur; less = 0; eq = 0; }
     __device__ __forceinline__ void step(T x) {
         bool isn = kisnan(v) || kisnan(x);
         less = isn ? knan<T>() : less;

@@ -11,7 +11,7 @@
 extern "C" {
 #endif
 
-#define KUN_GPU_MODULE_ABI 0x6b470002ull
+#define KUN_GPU_MODULE_ABI 0x6b470003ull
 
 typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
 typedef enum { KUN_BUF_INPUT = 0, KUN_BUF_OUTPUT = 1, KUN_BUF_TEMP = 2 } KunGpuBufferKind;
@@ -58,6 +58,7 @@ typedef struct {
     int32_t num_scratch;       /* private [length][S] buffers needed */
     int64_t state_bytes_per_stock; /* stream mode persistent state */
     KunGpuLaunchFn launch;
+    int32_t num_kernels;       /* CUDA kernels one launch enqueues */
 } KunGpuStageDesc;
 
 typedef struct {

@@ -68,11 +68,22 @@ struct Arena {
 
 // Static execution plan of one module for a (num_stocks, length) shape.
 struct Plan {
-    std::vector<int> order;                 // stage ids in launch order
+    std::vector<int> order;                 // stage ids in a topological order
+    std::vector<std::vector<int>> preds;    // stage -> stages producing its inputs
     std::vector<int> temp_slot;             // per buffer: arena slot or -1
     std::vector<std::vector<int>> scratch;  // per stage: slots of its scratch
+    std::vector<int> stream_of;             // per stage: stream index
+    int num_streams = 1;
     int num_slots = 0;
     size_t slot_bytes = 0;
+};
+
+// A captured CUDA graph of one run, valid for the exact buffers it was
+// captured with.
+struct GraphEntry {
+    std::vector<void *> key;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;
 };
 
 struct Executor {
@@ -83,13 +94,24 @@ struct Executor {
     Arena staging;
     int32_t *d_error = nullptr;
     int64_t last_launches = 0;
-    std::map<std::tuple<const void *, long long, long long>, Plan> plans;
+    std::map<std::tuple<const void *, long long, long long, int>, Plan> plans;
     std::mutex mu;
     // optional per-stage timing (CUDA events around every launch)
     bool profile = false;
     std::vector<cudaEvent_t> ev;
     std::vector<int> ev_stage;
-    cudaStream_t stream() const { return user_stream ? user_stream : streams[0]; }
+    // stage completion events for cross-stream dependencies
+    std::vector<cudaEvent_t> done;
+    cudaEvent_t fork = nullptr;
+    // graph replay: a run whose key was seen before is captured once
+    bool use_graphs = true;
+    std::map<std::vector<void *>, int> seen;
+    std::vector<GraphEntry> graphs;
+    // ordering with a caller's stream: work always runs on streams[0] and is
+    // bridged to the caller's stream with these events
+    bool has_user_stream = false;
+    cudaEvent_t bridge_in = nullptr, bridge_out = nullptr;
+    cudaStream_t stream() const { return streams[0]; }
 };
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
@@ -114,58 +136,112 @@ static bool topo_order(const KunGpuModuleDesc *m, std::vector<int> &order) {
     return (int)order.size() == m->num_stages;
 }
 
-// Liveness-based slot assignment of temporaries and stage scratch.
-static bool make_plan(const KunGpuModuleDesc *m, long long S, long long length, Plan &p) {
+// Plan: topological order, stage -> stream assignment and slot assignment of
+// temporaries and scratch.  A slot is reused by stage P only when every stage
+// that last touched it is an ancestor of P in the stage DAG, so the plan is
+// safe however the streams interleave (the reference frees a temporary on its
+// last deref, cpp/Kun/Runtime.cpp:84-93).
+static bool make_plan(const KunGpuModuleDesc *m, long long S, long long length, int nstreams, Plan &p) {
     if (!topo_order(m, p.order)) {
         set_error("module %s: cyclic stage graph", m->name);
         return false;
     }
+    int ns = m->num_stages;
+    p.preds.assign(ns, {});
+    for (int i = 0; i < ns; i++) {
+        const KunGpuStageDesc &s = m->stages[i];
+        for (int d = 0; d < s.num_deps; d++)
+            if (s.deps[d] >= 0) p.preds[s.deps[d]].push_back(i);
+    }
+    int words = (ns + 63) / 64;
+    std::vector<std::vector<uint64_t>> anc(ns, std::vector<uint64_t>(words, 0));
+    for (int i : p.order)
+        for (int d : p.preds[i]) {
+            anc[i][d / 64] |= 1ull << (d % 64);
+            for (int w = 0; w < words; w++) anc[i][w] |= anc[d][w];
+        }
+    auto is_anc = [&](int a, int of) { return (anc[of][a / 64] >> (a % 64)) & 1ull; };
     size_t elem = m->dtype == 0 ? 4 : 8;
     p.slot_bytes = align_up((size_t)S * (size_t)length * elem, 256);
     int nb = m->num_buffers;
-    std::vector<int> last_use(nb, -1), producer_pos(nb, -1);
-    for (int pos = 0; pos < (int)p.order.size(); pos++) {
-        const KunGpuStageDesc &s = m->stages[p.order[pos]];
-        for (int k = 0; k < s.num_in; k++) last_use[s.in_bufs[k]] = pos;
-        for (int k = 0; k < s.num_out; k++) producer_pos[s.out_bufs[k]] = pos;
-    }
-    p.temp_slot.assign(nb, -1);
-    p.scratch.assign(m->num_stages, {});
-    std::vector<int> free_slots;
-    int next = 0;
-    auto take = [&]() {
-        if (!free_slots.empty()) {
-            int s = free_slots.back();
-            free_slots.pop_back();
-            return s;
+    std::vector<std::vector<int>> consumers(nb);
+    for (int i = 0; i < ns; i++) {
+        const KunGpuStageDesc &s = m->stages[i];
+        for (int k = 0; k < s.num_in; k++) {
+            int b = s.in_bufs[k];
+            if (std::find(consumers[b].begin(), consumers[b].end(), i) == consumers[b].end())
+                consumers[b].push_back(i);
         }
-        return next++;
+    }
+    std::vector<int> remaining(nb);
+    for (int b = 0; b < nb; b++) remaining[b] = (int)consumers[b].size();
+    p.temp_slot.assign(nb, -1);
+    p.scratch.assign(ns, {});
+    struct Slot {
+        bool busy = false;
+        std::vector<int> releasers;
     };
-    for (int pos = 0; pos < (int)p.order.size(); pos++) {
-        int si = p.order[pos];
+    std::vector<Slot> slots;
+    auto take = [&](int stage) {
+        for (size_t k = 0; k < slots.size(); k++) {
+            if (slots[k].busy) continue;
+            bool ok = true;
+            for (int r : slots[k].releasers)
+                if (!is_anc(r, stage)) { ok = false; break; }
+            if (ok) {
+                slots[k].busy = true;
+                return (int)k;
+            }
+        }
+        slots.push_back(Slot());
+        slots.back().busy = true;
+        return (int)slots.size() - 1;
+    };
+    for (int si : p.order) {
         const KunGpuStageDesc &s = m->stages[si];
         for (int k = 0; k < s.num_out; k++) {
             int b = s.out_bufs[k];
-            if (m->buffers[b].kind == KUN_BUF_TEMP) p.temp_slot[b] = take();
+            if (m->buffers[b].kind == KUN_BUF_TEMP) p.temp_slot[b] = take(si);
         }
-        for (int k = 0; k < s.num_scratch; k++) p.scratch[si].push_back(take());
-        // release scratch and temps whose last consumer is this stage
-        for (int sl : p.scratch[si]) free_slots.push_back(sl);
+        for (int k = 0; k < s.num_scratch; k++) p.scratch[si].push_back(take(si));
+        for (int sl : p.scratch[si]) {
+            slots[sl].busy = false;
+            slots[sl].releasers = {si};
+        }
         for (int k = 0; k < s.num_in; k++) {
             int b = s.in_bufs[k];
-            if (m->buffers[b].kind == KUN_BUF_TEMP && last_use[b] == pos && p.temp_slot[b] >= 0) {
-                bool dup = false;
-                for (int q = 0; q < k; q++) dup |= s.in_bufs[q] == b;
-                if (!dup) free_slots.push_back(p.temp_slot[b]);
+            bool first = true;
+            for (int q = 0; q < k; q++) first &= s.in_bufs[q] != b;
+            if (!first || m->buffers[b].kind != KUN_BUF_TEMP || p.temp_slot[b] < 0) continue;
+            if (--remaining[b] == 0) {
+                slots[p.temp_slot[b]].busy = false;
+                slots[p.temp_slot[b]].releasers = consumers[b];
             }
         }
-        // a temp nobody reads is dead right away
         for (int k = 0; k < s.num_out; k++) {
             int b = s.out_bufs[k];
-            if (m->buffers[b].kind == KUN_BUF_TEMP && last_use[b] < 0) free_slots.push_back(p.temp_slot[b]);
+            if (m->buffers[b].kind == KUN_BUF_TEMP && consumers[b].empty()) {
+                slots[p.temp_slot[b]].busy = false;
+                slots[p.temp_slot[b]].releasers = {si};
+            }
         }
     }
-    p.num_slots = next;
+    p.num_slots = (int)slots.size();
+    // streams: continue a predecessor's chain when it is that stream's tail,
+    // otherwise take the stream with the least work queued
+    p.num_streams = std::max(1, nstreams);
+    p.stream_of.assign(ns, 0);
+    std::vector<int> tail(p.num_streams, -1), load(p.num_streams, 0);
+    for (int si : p.order) {
+        int pick = -1;
+        for (int d : p.preds[si])
+            for (int k = 0; k < p.num_streams; k++)
+                if (tail[k] == d) pick = k;
+        if (pick < 0) pick = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        p.stream_of[si] = pick;
+        tail[pick] = si;
+        load[pick] += m->stages[si].num_kernels > 0 ? m->stages[si].num_kernels : 1;
+    }
     return true;
 }
 
@@ -189,6 +265,72 @@ static size_t user_buffer_elems(const KunGpuModuleDesc *m, const KunGpuBufferDes
     if (layout == KUN_LAYOUT_STS) cols = (S + m->blocking_len - 1) / m->blocking_len * m->blocking_len;
     if (input && !strncmp(b.name, "__init", 6)) rows = 1;
     return (size_t)rows * (size_t)cols;
+}
+
+static void ensure_events(std::vector<cudaEvent_t> &v, size_t n, unsigned flags) {
+    while (v.size() < n) {
+        cudaEvent_t e;
+        cudaEventCreateWithFlags(&e, flags);
+        v.push_back(e);
+    }
+}
+
+// Enqueue all stages.  Single stream: in plan order.  Several streams: each
+// stage on its assigned stream after its predecessors' completion events.
+static KunStatus enqueue_stages(Executor *ex, const KunGpuModuleDesc *m, const Plan &plan, void **ptrs,
+                                long long S, long long total_time, long long cur_time, long long length,
+                                cudaStream_t origin, bool multi, int64_t &launches) {
+    std::vector<void *> scratch;
+    int ev_idx = 0;
+    if (ex->profile) {
+        ensure_events(ex->ev, plan.order.size() + 1, cudaEventDefault);
+        ex->ev_stage.assign(plan.order.begin(), plan.order.end());
+        cudaEventRecord(ex->ev[0], origin);
+    }
+    if (multi) {
+        ensure_events(ex->done, m->num_stages, cudaEventDisableTiming);
+        if (!ex->fork) cudaEventCreateWithFlags(&ex->fork, cudaEventDisableTiming);
+        cudaEventRecord(ex->fork, origin);
+        for (int k = 0; k < plan.num_streams; k++)
+            if (ex->streams[k] != origin) cudaStreamWaitEvent(ex->streams[k], ex->fork, 0);
+    }
+    std::vector<int> last_on(plan.num_streams, -1);
+    for (int si : plan.order) {
+        const KunGpuStageDesc &s = m->stages[si];
+        cudaStream_t st = origin;
+        if (multi) {
+            int k = plan.stream_of[si];
+            st = (k == 0) ? origin : ex->streams[k];
+            for (int d : plan.preds[si])
+                if (plan.stream_of[d] != k) cudaStreamWaitEvent(st, ex->done[d], 0);
+        }
+        scratch.clear();
+        for (int sl : plan.scratch[si]) scratch.push_back((char *)ex->arena.ptr + plan.slot_bytes * (size_t)sl);
+        KunGpuStageArgs a;
+        memset(&a, 0, sizeof a);
+        a.buffers = ptrs;
+        a.scratch = scratch.data();
+        a.num_stocks = S;
+        a.total_time = total_time;
+        a.start = cur_time;
+        a.length = length;
+        a.error_flag = ex->d_error;
+        int rc = s.launch(&a, (void *)st);
+        launches += s.num_kernels > 0 ? s.num_kernels : 1;
+        if (rc != 0) {
+            set_error("stage %d (%s) launch failed: %s", si, s.name, cudaGetErrorString((cudaError_t)rc));
+            return KUN_CUDA_ERROR;
+        }
+        if (ex->profile) cudaEventRecord(ex->ev[++ev_idx], st);
+        if (multi) {
+            cudaEventRecord(ex->done[si], st);
+            last_on[plan.stream_of[si]] = si;
+        }
+    }
+    if (multi)
+        for (int k = 1; k < plan.num_streams; k++)
+            if (last_on[k] >= 0) cudaStreamWaitEvent(origin, ex->done[last_on[k]], 0);
+    return KUN_SUCCESS;
 }
 
 KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &names, long long S,
@@ -219,11 +361,13 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
     }
     std::lock_guard<std::mutex> lk(ex->mu);
     cudaSetDevice(ex->device);
-    auto key = std::make_tuple((const void *)m, S, length);
+    bool multi = ex->streams.size() > 1 && !ex->profile;
+    int nstreams = multi ? (int)ex->streams.size() : 1;
+    auto key = std::make_tuple((const void *)m, S, length, nstreams);
     auto it = ex->plans.find(key);
     if (it == ex->plans.end()) {
         Plan p;
-        if (!make_plan(m, S, length, p)) return KUN_INVALID_ARGUMENT;
+        if (!make_plan(m, S, length, nstreams, p)) return KUN_INVALID_ARGUMENT;
         it = ex->plans.emplace(key, std::move(p)).first;
     }
     const Plan &plan = it->second;
@@ -233,6 +377,10 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
         return KUN_OUT_OF_MEMORY;
     }
     cudaStream_t st = ex->stream();
+    if (ex->has_user_stream) {
+        cudaEventRecord(ex->bridge_in, ex->user_stream);
+        cudaStreamWaitEvent(st, ex->bridge_in, 0);
+    }
     // resolve user buffers; stage host ones
     std::vector<void *> ptrs(m->num_buffers, nullptr);
     struct HostCopy {
@@ -276,39 +424,68 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
         for (auto &hc : host_out) ptrs[hc.buf] = (char *)ex->staging.ptr + hc.off;
     }
     int64_t launches = 0;
-    std::vector<void *> scratch;
-    if (ex->profile) {
-        while (ex->ev.size() < plan.order.size() + 1) {
-            cudaEvent_t e;
-            cudaEventCreate(&e);
-            ex->ev.push_back(e);
+    // graph key: module, shape and every device address the kernels see
+    std::vector<void *> gkey(ptrs.begin(), ptrs.end());
+    gkey.push_back((void *)m);
+    gkey.push_back((void *)(intptr_t)S);
+    gkey.push_back((void *)(intptr_t)total_time);
+    gkey.push_back((void *)(intptr_t)cur_time);
+    gkey.push_back((void *)(intptr_t)length);
+    gkey.push_back(ex->arena.ptr);
+    gkey.push_back((void *)(intptr_t)nstreams);
+    KunStatus rs = KUN_SUCCESS;
+    GraphEntry *ge = nullptr;
+    if (ex->use_graphs && !ex->profile) {
+        for (auto &g : ex->graphs)
+            if (g.key == gkey) ge = &g;
+        if (!ge && ++ex->seen[gkey] >= 2) {
+            // second run with these buffers: capture it once
+            cudaStreamCaptureStatus cs;
+            cudaStreamIsCapturing(st, &cs);
+            if (cs == cudaStreamCaptureStatusNone &&
+                cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                int64_t l2 = 0;
+                rs = enqueue_stages(ex, m, plan, ptrs.data(), S, total_time, cur_time, length, st, multi, l2);
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamEndCapture(st, &g);
+                cudaGraphExec_t exec = nullptr;
+                if (rs == KUN_SUCCESS && e == cudaSuccess && g &&
+                    cudaGraphInstantiate(&exec, g, 0) == cudaSuccess) {
+                    GraphEntry ent;
+                    ent.key = gkey;
+                    ent.exec = exec;
+                    ent.launches = l2;
+                    if (ex->graphs.size() >= 16) {
+                        cudaGraphExecDestroy(ex->graphs.front().exec);
+                        ex->graphs.erase(ex->graphs.begin());
+                    }
+                    ex->graphs.push_back(ent);
+                    ge = &ex->graphs.back();
+                } else {
+                    cudaGetLastError();
+                }
+                if (g) cudaGraphDestroy(g);
+                if (rs != KUN_SUCCESS) return rs;
+            }
         }
-        ex->ev_stage.assign(plan.order.begin(), plan.order.end());
-        cudaEventRecord(ex->ev[0], st);
     }
-    for (int si : plan.order) {
-        const KunGpuStageDesc &s = m->stages[si];
-        scratch.clear();
-        for (int sl : plan.scratch[si]) scratch.push_back((char *)ex->arena.ptr + plan.slot_bytes * (size_t)sl);
-        KunGpuStageArgs a;
-        memset(&a, 0, sizeof a);
-        a.buffers = ptrs.data();
-        a.scratch = scratch.data();
-        a.num_stocks = S;
-        a.total_time = total_time;
-        a.start = cur_time;
-        a.length = length;
-        a.error_flag = ex->d_error;
-        int rc = s.launch(&a, (void *)st);
-        launches++;
-        if (ex->profile) cudaEventRecord(ex->ev[launches], st);
-        if (rc != 0) {
-            set_error("stage %d (%s) launch failed: %s", si, s.name, cudaGetErrorString((cudaError_t)rc));
+    if (ge) {
+        cudaError_t e = cudaGraphLaunch(ge->exec, st);
+        if (e != cudaSuccess) {
+            set_error("graph launch failed: %s", cudaGetErrorString(e));
             return KUN_CUDA_ERROR;
         }
+        launches = ge->launches;
+    } else {
+        rs = enqueue_stages(ex, m, plan, ptrs.data(), S, total_time, cur_time, length, st, multi, launches);
+        if (rs != KUN_SUCCESS) return rs;
     }
     ex->last_launches = launches;
     for (auto &hc : host_out) cudaMemcpyAsync(hc.host, ptrs[hc.buf], hc.bytes, cudaMemcpyDeviceToHost, st);
+    if (ex->has_user_stream) {
+        cudaEventRecord(ex->bridge_out, st);
+        cudaStreamWaitEvent(ex->user_stream, ex->bridge_out, 0);
+    }
     if (sync || !host_in.empty() || !host_out.empty()) {
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
@@ -344,6 +521,12 @@ void destroy_executor(Executor *ex) {
         cudaStreamSynchronize(s);
         cudaStreamDestroy(s);
     }
+    for (auto &g : ex->graphs) cudaGraphExecDestroy(g.exec);
+    for (auto e : ex->ev) cudaEventDestroy(e);
+    for (auto e : ex->done) cudaEventDestroy(e);
+    if (ex->fork) cudaEventDestroy(ex->fork);
+    if (ex->bridge_in) cudaEventDestroy(ex->bridge_in);
+    if (ex->bridge_out) cudaEventDestroy(ex->bridge_out);
     if (ex->d_error) cudaFree(ex->d_error);
     delete ex;
 }
@@ -422,7 +605,23 @@ KUN_EXPORT void kunRunGraph(KunExecutorHandle exec, KunModuleHandle m, KunBuffer
 KUN_EXPORT KunStatus kunExecutorSetStream(KunExecutorHandle exec, void *cuda_stream) {
     auto *ex = (Executor *)exec;
     if (!ex) return KUN_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ex->mu);
+    if (!ex->bridge_in) {
+        cudaEventCreateWithFlags(&ex->bridge_in, cudaEventDisableTiming);
+        cudaEventCreateWithFlags(&ex->bridge_out, cudaEventDisableTiming);
+    }
     ex->user_stream = (cudaStream_t)cuda_stream;
+    ex->has_user_stream = true;
+    return KUN_SUCCESS;
+}
+
+// Stop ordering with a caller's stream.
+KUN_EXPORT KunStatus kunExecutorClearStream(KunExecutorHandle exec) {
+    auto *ex = (Executor *)exec;
+    if (!ex) return KUN_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(ex->mu);
+    ex->has_user_stream = false;
+    ex->user_stream = nullptr;
     return KUN_SUCCESS;
 }
 
@@ -434,6 +633,14 @@ KUN_EXPORT KunStatus kunExecutorSynchronize(KunExecutorHandle exec) {
         set_error("CUDA error: %s", cudaGetErrorString(e));
         return KUN_CUDA_ERROR;
     }
+    return KUN_SUCCESS;
+}
+
+// Capture repeated runs into CUDA graphs (default on).
+KUN_EXPORT KunStatus kunExecutorSetGraphs(KunExecutorHandle exec, int enable) {
+    auto *ex = (Executor *)exec;
+    if (!ex) return KUN_INVALID_ARGUMENT;
+    ex->use_graphs = enable != 0;
     return KUN_SUCCESS;
 }
 

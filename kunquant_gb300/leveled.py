@@ -265,6 +265,8 @@ from .codegen import StageGen  # noqa: E402
 
 PAR_CHUNK = 32
 REG_WINDOW_MAX = 64
+VEC_U = 4
+SCAN_BLOCK = 16
 
 
 class LeveledGen(StageGen):
@@ -276,12 +278,20 @@ class LeveledGen(StageGen):
         self.fplan = contraction.plan(self.ops)
         self.cur_level = None
         self.cur_comp: Set[int] = set()
+        self.vec = False
+        self.pf_window = None
+        self.mats: Set[int] = set()
 
     def val(self, i: int) -> str:
         if self.cur_level is not None and self.ops[i].get("p", -1) < 0:
             i = self.plan.value_source(i, self.cur_level)
+        top = self.ops[i].get("p", -1) < 0
         if self.ops[i]["k"] in REDUCTIONS and i not in self.cur_comp:
-            return f"v{i}"  # materialised at an earlier level, loaded per row
+            return f"v{i}[u]" if self.vec else f"v{i}"  # materialised earlier, loaded per row
+        if self.vec and top:
+            if self.ops[i]["k"] in REDUCTIONS:
+                return f"r{i}[u].value()"
+            return f"v{i}[u]"
         return super().val(i)
 
     # ------------------------------------------------------------------ memory
@@ -535,6 +545,193 @@ class LeveledGen(StageGen):
         for i in stores:
             self.lines.append(f"{ind}b{i}[t * st{i}] = {self.val(i)};")
 
+    def window_read(self, src: int, off) -> str:
+        key = (src, str(off))
+        if self.pf_window is not None and key in self.pf_window:
+            return f"{self.pf_window[key]}[u]"
+        return super().window_read(src, off)
+
+    def _scan_prefetch(self, role: dict, B: int, ind: str):
+        """Scan role body: rows are processed in blocks of B; every series the
+        role reads (values at t and fixed-offset windowed reads) is loaded for
+        the whole block first, so the B sequential state updates never wait on
+        memory."""
+        ops, T = self.ops, self.T
+        comp, vr = role["comp"], role["vr"]
+        stores = [i for i in role["roots"] if i in self.mats]
+        L = self.lines
+        self.cur_comp = comp
+        wins = {}
+        for i in sorted(comp):
+            k = ops[i]["k"]
+            if k in ("FastWindowedSum", "WindowedLinearRegression", "BackRef"):
+                wins[(ops[i]["in"][0], str(ops[i]["window"]))] = f"pw{i}"
+        L.append(f"{ind}for (long long tb = 0; tb < length; tb += {B}) {{")
+        bi = ind + "  "
+        for j in sorted(vr):
+            if ops[j]["k"] == "Input" and ops[j].get("single_value"):
+                L.append(f"{bi}const {T} pv{j} = b{j}[0];")
+                continue
+            L.append(f"{bi}{T} pv{j}[{B}];")
+            L.append(f"{bi}#pragma unroll")
+            L.append(f"{bi}for (int u = 0; u < {B}; ++u) pv{j}[u] = (tb + u < length) ? b{j}[(tb + u) * st{j}] : kun::knan<{T}>();")
+        done = set()
+        for (src, off), name in wins.items():
+            if name in done:
+                continue
+            done.add(name)
+            L.append(f"{bi}{T} {name}[{B}];")
+            L.append(f"{bi}#pragma unroll")
+            L.append(f"{bi}for (int u = 0; u < {B}; ++u) {{ const long long r = tb + u - {off}; "
+                     f"{name}[u] = (r >= 0 && tb + u < length) ? b{src}[r * st{src}] : kun::knan<{T}>(); }}")
+        L.append(f"{bi}#pragma unroll")
+        L.append(f"{bi}for (int u = 0; u < {B}; ++u) {{")
+        bj = bi + "  "
+        L.append(f"{bj}const long long t = tb + u;")
+        L.append(f"{bj}if (t >= length) break;")
+        for j in sorted(vr):
+            if ops[j]["k"] == "Input" and ops[j].get("single_value"):
+                L.append(f"{bj}const {T} v{j} = pv{j};")
+            else:
+                L.append(f"{bj}const {T} v{j} = pv{j}[u];")
+        self.pf_window = wins
+        loops = self._loops()
+        for i in range(len(ops)):
+            if i in comp and ops[i].get("p", -1) < 0:
+                self.emit_top(i, bj, loops, comp)
+        self.pf_window = None
+        for i in stores:
+            L.append(f"{bj}b{i}[t * st{i}] = {self.val(i)};")
+        L.append(f"{bi}}}")
+        L.append(f"{ind}}}")
+
+    # ------------------------------------------------------------------ vector form
+    def _vload(self, j: int, texpr: str) -> str:
+        """Guarded read of series j at row `texpr` (NaN outside [0, length))."""
+        return (f"(((long long)({texpr}) >= 0 && (long long)({texpr}) < length) ? "
+                f"b{j}[(long long)({texpr}) * st{j}] : kun::knan<{self.T}>())")
+
+    def _emit_par_vec(self, comp: Set[int], vr: Set[int], stores: List[int], loops, U: int, ind: str):
+        ops, T = self.ops, self.T
+        self.cur_comp = comp
+        self.vec = True
+        L = self.lines
+        for j in sorted(vr):
+            if ops[j]["k"] == "Input" and ops[j].get("single_value"):
+                L.append(f"{ind}{T} v{j}[{U}]; for (int u = 0; u < {U}; ++u) v{j}[u] = b{j}[0];")
+            else:
+                L.append(f"{ind}{T} v{j}[{U}];")
+                L.append(f"{ind}#pragma unroll")
+                L.append(f"{ind}for (int u = 0; u < {U}; ++u) v{j}[u] = {self._vload(j, 't + u')};")
+        queues: Dict[Tuple[int, int], str] = {}
+        chain_head = {}
+        for i in range(len(ops)):
+            if ops[i]["k"] == "ForeachBackWindow":
+                chain_head[i] = self.plan.loop_chain[i][0]
+        fplan = self.fplan
+        for i in range(len(ops)):
+            if i not in comp or ops[i].get("p", -1) >= 0:
+                continue
+            op = ops[i]
+            k = op["k"]
+            a = op["in"]
+            if k == "Input":
+                continue
+            if k in ("Output", "WindowedTempOutput"):
+                L.append(f"{ind}{T} v{i}[{U}];")
+                L.append(f"{ind}#pragma unroll")
+                L.append(f"{ind}for (int u = 0; u < {U}; ++u) {{ v{i}[u] = {self.val(a[0])}; "
+                         f"if (t + u < t1) b{i}[(t + u) * st{i}] = v{i}[u]; }}")
+            elif k == "ForeachBackWindow":
+                body, reds, own = loops[i]
+                w, seg = op["window"], op.get("segment_end", 0)
+                head = chain_head[i]
+                for r in own:
+                    rk = ops[r]["k"]
+                    decl = self.reduction_decl(r)
+                    if rk == "ReduceRank":
+                        L.append(f"{ind}kun::RRank<{T}> r{r}[{U}];")
+                        L.append(f"{ind}#pragma unroll")
+                        L.append(f"{ind}for (int u = 0; u < {U}; ++u) r{r}[u].reset({self.val(ops[r]['in'][1])});")
+                    else:
+                        L.append(f"{ind}{decl.split(' r')[0]} r{r}[{U}];")
+                srcs = sorted({ops[j]["in"][1] for j in body if ops[j]["k"] == "IterValue"})
+                for src in srcs:
+                    key = (head, src)
+                    if key not in queues:
+                        qn = f"q{head}_{src}"
+                        queues[key] = qn
+                        wh = ops[head]["window"]
+                        L.append(f"{ind}{T} {qn}[{U}];")
+                        L.append(f"{ind}#pragma unroll")
+                        L.append(f"{ind}for (int u = 0; u < {U}; ++u) {qn}[u] = {self._vload(src, f't + u - {wh - 1}')};")
+                L.append(f"{ind}#pragma unroll 2")
+                L.append(f"{ind}for (int iter = {w - 1}; iter >= {seg}; --iter) {{")
+                bi = ind + "  "
+                L.append(f"{bi}#pragma unroll")
+                L.append(f"{bi}for (int u = 0; u < {U}; ++u) {{")
+                bj = bi + "  "
+                for j in body:
+                    bo = ops[j]
+                    if bo["k"] == "IterValue":
+                        L.append(f"{bj}const {T} v{j} = {queues[(head, bo['in'][1])]}[u];")
+                    elif bo["k"] == "WindowLoopIndex":
+                        L.append(f"{bj}const {T} v{j} = ({T})({bo.get('loop_window', w)} - 1 - iter);")
+                    else:
+                        e = self.simple_expr(j, fplan)
+                        if e is None:
+                            raise Unsupported(f"op in loop body: {bo['k']}")
+                        L.append(f"{bj}const {T} v{j} = {e};")
+                for r in reds:
+                    self._vstep(r, bj)
+                L.append(f"{bi}}}")
+                for src in srcs:
+                    qn = queues[(head, src)]
+                    L.append(f"{bi}#pragma unroll")
+                    L.append(f"{bi}for (int u = 0; u < {U - 1}; ++u) {qn}[u] = {qn}[u + 1];")
+                    L.append(f"{bi}{qn}[{U - 1}] = {self._vload(src, f't + {U} - iter')};")
+                L.append(f"{ind}}}")
+            elif k in REDUCTIONS:
+                pass
+            elif k == "BackRef":
+                L.append(f"{ind}{T} v{i}[{U}];")
+                L.append(f"{ind}#pragma unroll")
+                L.append(f"{ind}for (int u = 0; u < {U}; ++u) v{i}[u] = {self._vload(a[0], f't + u - {op['window']}')};")
+            else:
+                e = self.simple_expr(i, fplan)
+                if e is None:
+                    raise Unsupported(f"op {k} in a vector kernel")
+                L.append(f"{ind}{T} v{i}[{U}];")
+                L.append(f"{ind}#pragma unroll")
+                L.append(f"{ind}for (int u = 0; u < {U}; ++u) v{i}[u] = {e};")
+        for i in stores:
+            L.append(f"{ind}#pragma unroll")
+            L.append(f"{ind}for (int u = 0; u < {U}; ++u) if (t + u < t1) b{i}[(t + u) * st{i}] = {self.val(i)};")
+        self.vec = False
+
+    def _vstep(self, r: int, ind: str):
+        """Per-lane reduction step inside the lane loop."""
+        ops = self.ops
+        op = ops[r]
+        k = op["k"]
+        x = self.val(op["in"][0])
+        if k == "ReduceAdd" and r in self.fplan:
+            _, prod = self.fplan[r]
+            po = ops[prod]
+            A = self.val(po["in"][0])
+            B = self.val(po["in"][1]) if po["k"] == "Mul" else self.lit(po["value"])
+            loop = contraction.reduction_loop(ops, r)
+            if contraction.loop_unrolled(ops, loop):
+                first = ops[loop]["window"] - 1
+                self.lines.append(f"{ind}if (iter == {first}) r{r}[u].step_fma_first({A}, {B}); "
+                                  f"else r{r}[u].step_fma({A}, {B});")
+            else:
+                self.lines.append(f"{ind}r{r}[u].step_fma({A}, {B});")
+        elif k in ("ReduceArgMax", "ReduceArgMin"):
+            self.lines.append(f"{ind}r{r}[u].step({x}, iter);")
+        else:
+            self.lines.append(f"{ind}r{r}[u].step({x});")
+
     # ------------------------------------------------------------------ stage
     def gen_ts(self):
         ops, T = self.ops, self.T
@@ -550,6 +747,7 @@ class LeveledGen(StageGen):
             for g in groups:
                 reads |= g["vr"] | g["wr"]
         mats = sorted(j for j in reads if ops[j]["k"] not in ("Input", "Output", "WindowedTempOutput"))
+        self.mats = set(mats)
         for j in mats:
             self.scratch[j] = len(self.scratch)
         srcs, calls = [], []
@@ -588,8 +786,12 @@ class LeveledGen(StageGen):
                         self.lines.append(f"    sl{i}.step((t - {W} >= tw) ? {self.read_at(src, f't - {W}')} : kun::knan<{T}>(), "
                                           f"{self.read_at(src, 't')}, (int)t);")
                     self.lines.append("  }")
-                self.lines.append("  for (long long t = t0; t < t1; ++t) {")
-                self._body(comp, vr, stores, loops, "    ")
+                if sls or VEC_U <= 1:
+                    self.lines.append("  for (long long t = t0; t < t1; ++t) {")
+                    self._body(comp, vr, stores, loops, "    ")
+                else:
+                    self.lines.append(f"  for (long long t = t0; t < t1; t += {VEC_U}) {{")
+                    self._emit_par_vec(comp, vr, stores, loops, VEC_U, "    ")
                 self.lines.append("  }")
                 grid_y = f"(unsigned)((a->length + {chunk} - 1) / {chunk})"
             else:
@@ -609,10 +811,7 @@ class LeveledGen(StageGen):
                         sd = self._state_decl(i)
                         if sd:
                             self.lines.append(f"    {sd}")
-                    self.lines.append("    for (long long t = 0; t < length; ++t) {")
-                    stores = [i for i in r["roots"] if i in mats]
-                    self._body(r["comp"], r["vr"], stores, loops, "      ")
-                    self.lines.append("    }")
+                    self._scan_prefetch(r, SCAN_BLOCK, "    ")
                     self.lines.append("  } break;")
                 self.lines.append("  default: break;")
                 self.lines.append("  }")

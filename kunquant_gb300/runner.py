@@ -49,9 +49,11 @@ def _load_runtime():
             "kunRunGraph": (None, [vp, vp, vp, sz, sz, sz, sz]),
             "kunRunGraphEx": (i32, [vp, vp, vp, sz, sz, sz, sz, i32]),
             "kunExecutorSetStream": (i32, [vp, vp]),
+            "kunExecutorClearStream": (i32, [vp]),
             "kunExecutorSynchronize": (i32, [vp]),
             "kunExecutorLastLaunchCount": (i64, [vp]),
             "kunExecutorSetProfiling": (i32, [vp, i32]),
+            "kunExecutorSetGraphs": (i32, [vp, i32]),
             "kunExecutorStageTimes": (i32, [vp, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_float), i32]),
             "kunGetLastError": (cp, []),
             "kunModuleNumBuffers": (i32, [vp]),
@@ -121,6 +123,9 @@ class Executor:
 
     def last_launch_count(self) -> int:
         return int(runtime().kunExecutorLastLaunchCount(self.handle))
+
+    def set_graphs(self, enable: bool):
+        _check(runtime().kunExecutorSetGraphs(self.handle, 1 if enable else 0))
 
     def set_profiling(self, enable: bool):
         _check(runtime().kunExecutorSetProfiling(self.handle, 1 if enable else 0))
@@ -315,7 +320,7 @@ def runGraph(exec: Executor, mod: Module, inputs: dict, cur_time: int, length: i
             import torch
             L.kunExecutorSetStream(exec.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
             rc = L.kunRunGraphEx(exec.handle, mod.handle, m, num_stocks, known_T, cur_time, length, 0)
-            L.kunExecutorSetStream(exec.handle, None)
+            L.kunExecutorClearStream(exec.handle)
         else:
             rc = L.kunRunGraphEx(exec.handle, mod.handle, m, num_stocks, known_T, cur_time, length, 1)
         _check(rc)

@@ -66,3 +66,24 @@ def test_torch_device_path_bit_exact():
     got = {k: v.cpu().numpy() for k, v in got.items()}
     bad = compare_exact(got, want)
     assert not bad, f"{len(bad)} outputs differ: {dict(list(bad.items())[:5])}"
+
+
+@pytest.mark.gpu
+def test_multistream_graph_replay_bit_exact():
+    """Concurrent stages on 4 streams; the third run replays a captured graph."""
+    import torch
+    key, name, S, T = "alpha101_f32", "alpha101", 96, 260
+    data = synth.ohlcv(S, T, seed=5, nan_frac=0.005)
+    want = _oracle(key).run(data)
+    ex = kr.createMultiThreadExecutor(4)
+    mod = _module(key, name)
+    dev = {k: torch.from_numpy(v).cuda() for k, v in data.items()}
+    outs = {n: torch.empty((T, S), dtype=torch.float32, device="cuda") for n in mod.getOutputNames()}
+    for it in range(3):
+        for o in outs.values():
+            o.fill_(-7.0)
+        kr.runGraph(ex, mod, dev, 0, T, outputs=outs)
+        torch.cuda.synchronize()
+        got = {k: v.cpu().numpy() for k, v in outs.items()}
+        bad = compare_exact(got, want)
+        assert not bad, f"run {it}: {len(bad)} outputs differ: {dict(list(bad.items())[:5])}"
