@@ -138,8 +138,7 @@ __global__ void __launch_bounds__(256) diffwsum_rows(const T *__restrict__ in0, 
     for (long long t = blockIdx.x; t < length; t += gridDim.x) {
         if (threadIdx.x == 0) {
             T sum = 0;
-            // `sum += a * b` is contracted by the reference build
-            for (long long i = 0; i < S; i++) sum = kfma(in0[t * S + i], in1[t * S + i], sum);
+            for (long long i = 0; i < S; i++) sum = kadd(sum, kmul(in0[t * S + i], in1[t * S + i]));
             total = sum;
         }
         __syncthreads();

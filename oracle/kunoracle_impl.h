@@ -792,8 +792,7 @@ static void SFX(scale_row)(const T *in, T *out, int64_t S) {
 /* DiffWithWeightedSum, KunQuant/ops/MiscOp.py:220-240 */
 static void SFX(diffw_row)(const T *in0, const T *in1, T *out, int64_t S) {
     T sum = 0;
-    /* `sum += a * b` is contracted by the reference build */
-    for (int64_t i = 0; i < S; i++) sum = FMA(in0[i], in1[i], sum);
+    for (int64_t i = 0; i < S; i++) sum += in0[i] * in1[i];
     for (int64_t i = 0; i < S; i++) out[i] = in0[i] - sum;
 }
 

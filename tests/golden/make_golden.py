@@ -1,0 +1,232 @@
+"""Generates the golden fixtures of tests/golden from the reference itself.
+
+Needs the reference sources (``$KUN_REFERENCE_ROOT``, default /root/reference):
+the reference CPU runtime is built by ``oracle/build_ref.py`` and its own JIT
+compiles every graph below.  For each case the fixture holds the inputs, the
+reference's outputs and the module spec the GPU backend compiles, so the tests
+need neither the reference nor its front end.
+
+    python tests/golden/make_golden.py            # all cases
+    python tests/golden/make_golden.py rank2 ...  # some cases
+
+The unit graphs follow the reference's own runtime tests
+(tests/test_runtime.py: rolling stats, argmin issue #19, rank with ties and
+NaN rows, bit-exact rank(x+x)+x and the alpha029 rank chain, log special
+values) plus graphs that reach the skip-list path (windows > 400 with 8 lanes)
+and the loop-index op (max drawdown).
+"""
+import gzip
+import io
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+
+def _graphs():
+    from KunQuant.Op import Builder, Input, Output, Rank, Scale, ConstantOp
+    from KunQuant.Stage import Function
+    from KunQuant.ops import (TsArgMin, TsArgMax, WindowedMin, WindowedMax, TsRank, WindowedStddev,
+                              WindowedCorrelation, WindowedCovariance, WindowedSum, WindowedAvg,
+                              WindowedQuantile, Log, Exp, DecayLinear, WindowedLinearRegressionSlope,
+                              ExpMovingAvg, WindowedMaxDrawdown, WindowedSkew, WindowedKurt, Pow,
+                              WindowedProduct, SetInfOrNanToValue, Sign, Abs, Select, DiffWithWeightedSum)
+
+    def mk(body):
+        def build():
+            b = Builder()
+            with b:
+                body()
+            return Function(b.ops)
+        return build
+
+    def argmin():
+        a = Input("a")
+        Output(TsArgMin(a, 5), "ou2")
+        Output(WindowedMin(a, 5), "tsmin")
+        Output(TsRank(a, 5), "tsrank")
+
+    def rank():
+        Output(Rank(Input("a")), "ou2")
+
+    def rank2():
+        a = Input("a")
+        Output(Rank(a + a) + a, "out")
+
+    def rank029():
+        a = Input("a")
+        inner = WindowedSum(Rank(Rank(-1 * Rank(a))), 5)
+        Output(inner, "ou1")
+        Output(Rank(inner), "ou2")
+
+    def logexp():
+        a = Input("a")
+        Output(Log(a), "outlog")
+        Output(Exp(a), "outexp")
+
+    def stats():
+        a, b = Input("a"), Input("b")
+        Output(WindowedAvg(a, 10), "avg")
+        Output(WindowedStddev(a, 10), "std")
+        Output(WindowedCorrelation(a, 10, b), "corr")
+        Output(WindowedCovariance(a, 20, b), "cov")
+        Output(WindowedQuantile(a, 10, 0.49), "q49")
+        Output(DecayLinear(a, 7), "decay")
+        Output(WindowedLinearRegressionSlope(a, 12), "slope")
+        Output(WindowedProduct(Abs(a) + 1, 6), "prod")
+        Output(TsArgMax(a, 200), "argmax200")
+        Output(WindowedMax(a, 200), "max200")
+        Output(TsRank(a, 200), "tsrank200")
+        Output(Sign(a - 0.5), "sign")
+        Output(Pow(Abs(a), ConstantOp(2.5)), "pow")
+        Output(Select(a > b, a, b * 2), "sel")
+        Output(SetInfOrNanToValue(a / (b - 0.5)), "infnan")
+
+    def skiplists():
+        a = Input("a")
+        Output(TsRank(a, 500), "tsrank500")
+        Output(TsArgMin(a, 450), "argmin450")
+        Output(TsArgMax(a, 450), "argmax450")
+        Output(WindowedMin(a, 430), "min430")
+        Output(WindowedMax(a, 430), "max430")
+        Output(WindowedQuantile(a, 420, 0.3), "q30")
+
+    def misc():
+        a, b = Input("a"), Input("b")
+        Output(ExpMovingAvg(a, 10), "ema")
+        Output(WindowedMaxDrawdown(a, 12), "mdd")
+        Output(WindowedSkew(a, 12), "skew")
+        Output(WindowedKurt(a, 12), "kurt")
+        Output(Scale(a - 0.5), "scale")
+        Output(DiffWithWeightedSum(a, b), "diffw")
+
+    return {
+        # name: (builder, config kwargs, input maker)
+        "argmin_issue19": (mk(argmin), dict(input_layout="TS", output_layout="TS"), "issue19"),
+        "rank_ties_nan": (mk(rank), dict(input_layout="TS", output_layout="TS"), "rank"),
+        "rank2_exact": (mk(rank2), dict(input_layout="TS", output_layout="TS"), "u24"),
+        "rank2_unaligned": (mk(rank2), dict(input_layout="TS", output_layout="TS"), "u20"),
+        "rank029_f64": (mk(rank029), dict(input_layout="TS", output_layout="TS", dtype="double",
+                                          options={"opt_reduce": True, "fast_log": True,
+                                                   "no_fast_stat": True}), "u20_300"),
+        "logexp_f32": (mk(logexp), dict(input_layout="TS", output_layout="TS",
+                                        options={"fast_log": True}), "special"),
+        "logexp_f64": (mk(logexp), dict(input_layout="TS", output_layout="TS", dtype="double",
+                                        options={"fast_log": True, "no_fast_stat": True}), "special"),
+        "stats_f32": (mk(stats), dict(input_layout="TS", output_layout="TS",
+                                      options={"opt_reduce": True}), "ab"),
+        "stats_f32_noopt": (mk(stats), dict(input_layout="TS", output_layout="TS",
+                                            options={"opt_reduce": False}), "ab"),
+        "skiplists_f32": (mk(skiplists), dict(input_layout="TS", output_layout="TS"), "long"),
+        "misc_f32": (mk(misc), dict(input_layout="TS", output_layout="TS",
+                                    options={"opt_reduce": True}), "ab"),
+    }
+
+
+def _inputs(kind, dtype):
+    rng = np.random.default_rng(2024)
+    if kind == "issue19":
+        data = [0.6898481863442985, 0.6992020600574415, 0.6992020600574417, 0.6968635916291558,
+                0.6968635916291558, 0.6968635916291558]
+        a = np.empty((6, 8), dtype)
+        for i in range(6):
+            a[i, :] = data[i]
+        return {"a": a}
+    if kind == "rank":
+        a = rng.random((20, 24)).astype(dtype)
+        a[3:9] = (np.arange(6)[:, None] // 2).astype(dtype)
+        a[10, :] = np.nan
+        a[12, ::3] = np.nan
+        a[14, :] = 0.0
+        a[14, ::2] = -0.0
+        return {"a": a}
+    if kind == "u24":
+        return {"a": rng.random((20, 24)).astype(dtype)}
+    if kind == "u20":
+        return {"a": rng.random((20, 20)).astype(dtype)}
+    if kind == "u20_300":
+        return {"a": rng.random((300, 20)).astype(dtype)}
+    if kind == "special":
+        vals = [0.0, -0.0, 1.0, -1.0, np.inf, -np.inf, np.nan, 88.7, 88.8, -87.3, -87.4, 1e-40,
+                1e-30, 3.4e38, 2.0, 0.5, 100.0, 1e5, 1e-5, 709.0, 710.0, -745.0]
+        extra = rng.uniform(-100, 100, 64 * 8 - len(vals))
+        return {"a": np.array(vals + list(extra), dtype=dtype).reshape(64, 8)}
+    if kind == "ab":
+        a = rng.random((260, 16)).astype(dtype)
+        b = rng.random((260, 16)).astype(dtype)
+        a[50:53, 3] = np.nan
+        a[100, :] = 0.5
+        b[120:124, 5] = np.nan
+        a[200:203, 7] = a[199, 7]
+        return {"a": a, "b": b}
+    if kind == "long":
+        a = rng.integers(0, 40, size=(600, 8)).astype(dtype) / 4
+        a[300:305, 2] = np.nan
+        return {"a": a}
+    raise KeyError(kind)
+
+
+def _save(name, spec, inputs, outputs, extra=None):
+    path = os.path.join(HERE, name + ".npz")
+    arrays = {"in__" + k: v for k, v in inputs.items()}
+    arrays.update({"out__" + k: v for k, v in outputs.items()})
+    buf = io.BytesIO()
+    np.savez_compressed(buf, **arrays)
+    with open(path, "wb") as f:
+        f.write(buf.getvalue())
+    meta = {"spec": spec}
+    meta.update(extra or {})
+    with gzip.GzipFile(os.path.join(HERE, name + ".json.gz"), "wb", mtime=0) as f:
+        f.write(json.dumps(meta, separators=(",", ":")).encode())
+    print(name, "->", os.path.relpath(path, REPO), os.path.getsize(path), "bytes")
+
+
+def predefined_cases():
+    from kunquant_gb300 import synth
+    from kunquant_gb300.graph import predefined_spec
+    return {
+        # fixture name: (library key, stocks, days, nan fraction, cur_time)
+        "alpha158_f32": ("alpha158_f32", 8, 160, 0.005, 0),
+        "alpha101_f32": ("alpha101_f32", 16, 200, 0.005, 0),
+        "alpha101_f32_start50": ("alpha101_f32", 16, 200, 0.0, 50),
+        "alpha158_f64": ("alpha158_f64", 4, 160, 0.005, 0),
+        "alpha101_f64": ("alpha101_f64", 8, 200, 0.005, 0),
+    }
+
+
+def main(names):
+    from oracle import refkun
+    from oracle.build_ref import import_reference
+    import_reference()
+    from kunquant_gb300 import synth
+    from kunquant_gb300.graph import predefined_spec
+    for name, (key, S, T, nanf, start) in predefined_cases().items():
+        if names and name not in names:
+            continue
+        spec = predefined_spec(key)
+        dt = np.float32 if spec["dtype"] == "float" else np.float64
+        data = synth.ohlcv(S, T, seed=S * 1000 + T, nan_frac=nanf, dtype=dt)
+        out = refkun.run_batch(key, data, cur_time=start, length=T - start)
+        _save(name, {"predefined": key}, data, out, {"cur_time": start})
+    if not names or "alpha101_stream_f32" in names:
+        key = "alpha101_stream_f32"
+        data = synth.ohlcv(8, 60, seed=99, nan_frac=0.0)
+        out = refkun.run_stream(key, data)
+        _save("alpha101_stream_f32", {"predefined": key}, data, out, {"stream": True})
+    for name, (build, cfg, kind) in _graphs().items():
+        if names and name not in names:
+            continue
+        spec, mod = refkun.compile_function("g_" + name, build, name, **cfg)
+        dt = np.float32 if spec["dtype"] == "float" else np.float64
+        inputs = _inputs(kind, dt)
+        out = refkun.run_module(mod, inputs)
+        _save(name, spec, inputs, out)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1:])

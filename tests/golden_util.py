@@ -1,0 +1,26 @@
+"""Loading of the golden fixtures written by tests/golden/make_golden.py."""
+import gzip
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def load(name):
+    """(spec, inputs, reference outputs, meta) of one fixture."""
+    with gzip.open(os.path.join(GOLDEN, name + ".json.gz"), "rb") as f:
+        meta = json.loads(f.read())
+    spec = meta["spec"]
+    if "predefined" in spec:
+        from kunquant_gb300.graph import predefined_spec
+        spec = predefined_spec(spec["predefined"])
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    inputs = {k[4:]: z[k] for k in z.files if k.startswith("in__")}
+    outputs = {k[5:]: z[k] for k in z.files if k.startswith("out__")}
+    return spec, inputs, outputs, meta
