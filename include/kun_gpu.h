@@ -155,6 +155,12 @@ int kunModuleNumStages(KunModuleHandle m);
 KunStatus kunStreamPushDataDevice(KunStreamContextHandle context, size_t handle, const void *device_buffer);
 const void *kunStreamGetCurrentBufferDevice(KunStreamContextHandle context, size_t handle);
 KunStatus kunStreamRunEx(KunStreamContextHandle context, int synchronize);
+/* Copy the current row of a buffer (num_stocks values) to device memory. */
+KunStatus kunStreamCopyCurrentDevice(KunStreamContextHandle context, size_t handle, void *device_dst);
+/* Ticks the stream has run (the time index of the next pushed row). */
+int64_t kunStreamTick(KunStreamContextHandle context);
+/* Device bytes one stock of a stream module holds (rings and op states). */
+int64_t kunStreamBytesPerStock(KunModuleHandle m);
 
 #ifdef __cplusplus
 }

@@ -475,6 +475,9 @@ extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
 
 def stage_generator(spec: dict, si: int, tag: str, mode: str = "leveled") -> StageGen:
     """Leveled kernels where the stage allows them, else the single-scan form."""
+    if spec["output_layout"] == "STREAM":
+        from .streamgen import StreamGen
+        return StreamGen(spec, si, tag)
     if mode == "leveled" and spec["stages"][si]["kind"] == "ts":
         from .leveled import LeveledGen, Unsupported
         try:
@@ -523,12 +526,21 @@ template <> struct LogTables<{T}> {{
     n_stages = len(spec["stages"])
     scratch_counts = [0] * n_stages
     kernel_counts = [1] * n_stages
+    state_t = [0] * n_stages
+    state_i = [0] * n_stages
+    init_fn = ["nullptr"] * n_stages
+    extern_init = []
     files: List[List[str]] = []
     cur: List[str] = []
     for si in range(n_stages):
-        src, nscr, nk = stage_generator(spec, si, tag, mode).generate()
+        g = stage_generator(spec, si, tag, mode)
+        src, nscr, nk = g.generate()
         scratch_counts[si] = nscr
         kernel_counts[si] = nk
+        state_t[si], state_i[si] = getattr(g, "state_t_vars", 0), getattr(g, "state_i_vars", 0)
+        if getattr(g, "has_init", False):
+            init_fn[si] = f"kst_{tag}_{si}_init"
+            extern_init.append(si)
         cur.append(src)
         if len(cur) >= stages_per_file:
             files.append(cur)
@@ -544,6 +556,8 @@ template <> struct LogTables<{T}> {{
     lines = [f"// generated module descriptor for {name}", '#include "kun_module_abi.h"', ""]
     for si in range(n_stages):
         lines.append(f'extern "C" int kst_{tag}_{si}_launch(const KunGpuStageArgs*, void*);')
+    for si in extern_init:
+        lines.append(f'extern "C" int kst_{tag}_{si}_init(const KunGpuStageArgs*, void*);')
     for si, st in enumerate(spec["stages"]):
         for key in ("in", "out", "deps"):
             vals = st.get(key, []) or []
@@ -555,7 +569,8 @@ template <> struct LogTables<{T}> {{
     for si, st in enumerate(spec["stages"]):
         lines.append(f"  {{{_c_str(st['name'][:200])}, {kinds[st['kind']]}, {len(st['in'])}, st{si}_in, "
                      f"{len(st['out'])}, st{si}_out, {len(st.get('deps', []))}, st{si}_deps, "
-                     f"{st.get('pending', 0)}, {scratch_counts[si]}, 0, kst_{tag}_{si}_launch, {kernel_counts[si]}}},")
+                     f"{st.get('pending', 0)}, {scratch_counts[si]}, 0, kst_{tag}_{si}_launch, {kernel_counts[si]}, "
+                     f"{state_t[si]}, {state_i[si]}, {init_fn[si]}}},")
     lines.append("};")
     bk = {"INPUT": "KUN_BUF_INPUT", "OUTPUT": "KUN_BUF_OUTPUT", "TEMP": "KUN_BUF_TEMP"}
     lines.append(f"static const KunGpuBufferDesc buffers_{tag}[] = {{")

@@ -11,7 +11,7 @@
 extern "C" {
 #endif
 
-#define KUN_GPU_MODULE_ABI 0x6b470003ull
+#define KUN_GPU_MODULE_ABI 0x6b470004ull
 
 typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
 typedef enum { KUN_BUF_INPUT = 0, KUN_BUF_OUTPUT = 1, KUN_BUF_TEMP = 2 } KunGpuBufferKind;
@@ -38,9 +38,20 @@ typedef struct {
     int64_t total_time;
     int64_t start;
     int64_t length;
-    const int32_t *ring_pos;   /* stream mode only (host array) */
-    void *state;               /* stream mode: per-stage persistent op state (device) */
+    const int32_t *ring_pos;   /* unused */
+    void *state;               /* stream mode: the stage's float/double state arrays */
     int32_t *error_flag;       /* device word; kernels set it instead of trapping */
+    /* stream mode: stocks live in rings of num_stocks (capacity) columns; a
+     * launch covers `nseg` segments (sessions): segment k holds stocks
+     * [seg_stock0[k], seg_stock0[k] + seg_off[k+1] - seg_off[k]) and is at
+     * tick seg_tick[k]; all three arrays are device memory */
+    void *state_i;             /* stream mode: the stage's int32 state arrays */
+    const int32_t *seg_off;
+    const int32_t *seg_stock0;
+    const int64_t *seg_tick;
+    int32_t nseg;
+    int64_t n_active;          /* seg_off[nseg] */
+    int32_t max_seg_len;       /* longest segment (cross-sectional stages) */
 } KunGpuStageArgs;
 
 typedef int (*KunGpuLaunchFn)(const KunGpuStageArgs *args, void *cuda_stream);
@@ -59,6 +70,11 @@ typedef struct {
     int64_t state_bytes_per_stock; /* stream mode persistent state */
     KunGpuLaunchFn launch;
     int32_t num_kernels;       /* CUDA kernels one launch enqueues */
+    /* stream mode: persistent state per stock and its initialiser, which
+     * resets stocks [seg_stock0[0], seg_stock0[0] + n_active) */
+    int32_t state_t_vars;      /* float/double arrays of num_stocks */
+    int32_t state_i_vars;      /* int32 arrays of num_stocks */
+    KunGpuLaunchFn init;
 } KunGpuStageDesc;
 
 typedef struct {

@@ -20,10 +20,7 @@
 #include <unordered_map>
 #include <vector>
 
-#include "kun_gpu.h"
-#include "kun_module_abi.h"
-
-#define KUN_EXPORT extern "C" __attribute__((visibility("default")))
+#include "kun_runtime_internal.h"
 
 namespace kungpu {
 
@@ -39,80 +36,6 @@ void set_error(const char *fmt, ...) {
 }
 void clear_error() { g_last_error.clear(); }
 const char *last_error() { return g_last_error.c_str(); }
-
-struct Library {
-    void *handle = nullptr;
-    std::string path;
-};
-
-struct Arena {
-    void *ptr = nullptr;
-    size_t bytes = 0;
-    ~Arena() {
-        if (ptr) cudaFree(ptr);
-    }
-    bool ensure(size_t need) {
-        if (need <= bytes) return true;
-        if (ptr) cudaFree(ptr);
-        ptr = nullptr;
-        bytes = 0;
-        if (need == 0) return true;
-        if (cudaMalloc(&ptr, need) != cudaSuccess) {
-            cudaGetLastError();
-            return false;
-        }
-        bytes = need;
-        return true;
-    }
-};
-
-// Static execution plan of one module for a (num_stocks, length) shape.
-struct Plan {
-    std::vector<int> order;                 // stage ids in a topological order
-    std::vector<std::vector<int>> preds;    // stage -> stages producing its inputs
-    std::vector<int> temp_slot;             // per buffer: arena slot or -1
-    std::vector<std::vector<int>> scratch;  // per stage: slots of its scratch
-    std::vector<int> stream_of;             // per stage: stream index
-    int num_streams = 1;
-    int num_slots = 0;
-    size_t slot_bytes = 0;
-};
-
-// A captured CUDA graph of one run, valid for the exact buffers it was
-// captured with.
-struct GraphEntry {
-    std::vector<void *> key;
-    cudaGraphExec_t exec = nullptr;
-    int64_t launches = 0;
-};
-
-struct Executor {
-    int device = 0;
-    std::vector<cudaStream_t> streams;
-    cudaStream_t user_stream = nullptr;
-    Arena arena;
-    Arena staging;
-    int32_t *d_error = nullptr;
-    int64_t last_launches = 0;
-    std::map<std::tuple<const void *, long long, long long, int>, Plan> plans;
-    std::mutex mu;
-    // optional per-stage timing (CUDA events around every launch)
-    bool profile = false;
-    std::vector<cudaEvent_t> ev;
-    std::vector<int> ev_stage;
-    // stage completion events for cross-stream dependencies
-    std::vector<cudaEvent_t> done;
-    cudaEvent_t fork = nullptr;
-    // graph replay: a run whose key was seen before is captured once
-    bool use_graphs = true;
-    std::map<std::vector<void *>, int> seen;
-    std::vector<GraphEntry> graphs;
-    // ordering with a caller's stream: work always runs on streams[0] and is
-    // bridged to the caller's stream with these events
-    bool has_user_stream = false;
-    cudaEvent_t bridge_in = nullptr, bridge_out = nullptr;
-    cudaStream_t stream() const { return streams[0]; }
-};
 
 static size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
@@ -689,29 +612,3 @@ KUN_EXPORT int kunModuleBlockingLen(KunModuleHandle m) { return M(m)->blocking_l
 KUN_EXPORT int kunModuleDtype(KunModuleHandle m) { return M(m)->dtype; }
 KUN_EXPORT int kunModuleNumStages(KunModuleHandle m) { return M(m)->num_stages; }
 
-// ---------------- stream API (filled in by kun_stream.cu when built) -------
-#ifndef KUN_HAVE_STREAM
-KUN_EXPORT KunStreamContextHandle kunCreateStream(KunExecutorHandle, KunModuleHandle, size_t) {
-    set_error("stream mode is not built");
-    return nullptr;
-}
-KUN_EXPORT KunStatus kunCreateStreamEx(KunExecutorHandle, KunModuleHandle, size_t, const KunStreamExtraArgs *,
-                                       KunStreamContextHandle *out) {
-    if (out) *out = nullptr;
-    set_error("stream mode is not built");
-    return KUN_INIT_ERROR;
-}
-KUN_EXPORT KunStatus kunStreamSerializeStates(KunStreamContextHandle, KunStateBufferKind, char *, size_t *) {
-    return KUN_INVALID_ARGUMENT;
-}
-KUN_EXPORT size_t kunQueryBufferHandle(KunStreamContextHandle, const char *) { return (size_t)-1; }
-KUN_EXPORT const float *kunStreamGetCurrentBuffer(KunStreamContextHandle, size_t) { return nullptr; }
-KUN_EXPORT void kunStreamPushData(KunStreamContextHandle, size_t, const float *) {}
-KUN_EXPORT void kunStreamRun(KunStreamContextHandle) {}
-KUN_EXPORT void kunDestoryStream(KunStreamContextHandle) {}
-KUN_EXPORT KunStatus kunStreamPushDataDevice(KunStreamContextHandle, size_t, const void *) {
-    return KUN_INVALID_ARGUMENT;
-}
-KUN_EXPORT const void *kunStreamGetCurrentBufferDevice(KunStreamContextHandle, size_t) { return nullptr; }
-KUN_EXPORT KunStatus kunStreamRunEx(KunStreamContextHandle, int) { return KUN_INVALID_ARGUMENT; }
-#endif

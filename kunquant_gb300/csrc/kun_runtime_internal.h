@@ -1,0 +1,112 @@
+// Internals shared by the runtime translation units of libkungpu.so.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "kun_gpu.h"
+#include "kun_module_abi.h"
+
+#define KUN_EXPORT extern "C" __attribute__((visibility("default")))
+
+namespace kungpu {
+
+void set_error(const char *fmt, ...);
+void clear_error();
+const char *last_error();
+
+struct Library {
+    void *handle = nullptr;
+    std::string path;
+};
+
+struct Arena {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    ~Arena() {
+        if (ptr) cudaFree(ptr);
+    }
+    bool ensure(size_t need) {
+        if (need <= bytes) return true;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        if (need == 0) return true;
+        if (cudaMalloc(&ptr, need) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        bytes = need;
+        return true;
+    }
+};
+
+// Static execution plan of one module for a (num_stocks, length) shape.
+struct Plan {
+    std::vector<int> order;                 // stage ids in a topological order
+    std::vector<std::vector<int>> preds;    // stage -> stages producing its inputs
+    std::vector<int> temp_slot;             // per buffer: arena slot or -1
+    std::vector<std::vector<int>> scratch;  // per stage: slots of its scratch
+    std::vector<int> stream_of;             // per stage: stream index
+    int num_streams = 1;
+    int num_slots = 0;
+    size_t slot_bytes = 0;
+};
+
+// A captured CUDA graph of one run, valid for the exact buffers it was
+// captured with.
+struct GraphEntry {
+    std::vector<void *> key;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;
+};
+
+struct Executor {
+    int device = 0;
+    std::vector<cudaStream_t> streams;
+    cudaStream_t user_stream = nullptr;
+    Arena arena;
+    Arena staging;
+    int32_t *d_error = nullptr;
+    int64_t last_launches = 0;
+    std::map<std::tuple<const void *, long long, long long, int>, Plan> plans;
+    std::mutex mu;
+    // optional per-stage timing (CUDA events around every launch)
+    bool profile = false;
+    std::vector<cudaEvent_t> ev;
+    std::vector<int> ev_stage;
+    // stage completion events for cross-stream dependencies
+    std::vector<cudaEvent_t> done;
+    cudaEvent_t fork = nullptr;
+    // graph replay: a run whose key was seen before is captured once
+    bool use_graphs = true;
+    std::map<std::vector<void *>, int> seen;
+    std::vector<GraphEntry> graphs;
+    // ordering with a caller's stream: work always runs on streams[0] and is
+    // bridged to the caller's stream with these events
+    bool has_user_stream = false;
+    cudaEvent_t bridge_in = nullptr, bridge_out = nullptr;
+    cudaStream_t stream() const { return streams[0]; }
+};
+
+// Device state of a stream module for `cap` stock columns: per buffer a ring
+// of `window` rows ([window][cap], row n % window holds tick n) and per stage
+// its op states as arrays of `cap` (float/double, then int32).
+struct StreamStore {
+    const KunGpuModuleDesc *m = nullptr;
+    long long cap = 0;
+    std::vector<void *> rings;
+    std::vector<void *> st_t, st_i;
+    void *d_init = nullptr;  // segment table of one reset
+    bool alloc(const KunGpuModuleDesc *mod, long long capacity);
+    void release();
+    size_t bytes_per_stock() const;
+    KunStatus reset(long long stock0, long long count, cudaStream_t st);
+};
+
+}  // namespace kungpu

@@ -1,0 +1,642 @@
+// Stream mode of libkungpu.so: the reference's StreamContext
+// (cpp/Kun/Runtime.cpp:385-546, C API cpp/Kun/CApi.cpp:79-189) on the GPU.
+//
+// A StreamStore holds the device state of a stream module for `cap` stock
+// columns: one ring of `window` rows per buffer (NaN filled, like
+// StreamBuffer::make) and, per stage, the struct-of-arrays state of its ops.
+// A stream context owns a store for its own stocks and replays one captured
+// CUDA graph per tick; the graph ends with a kernel that advances the
+// device-side tick counter, so ticks can be queued without host round trips.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "kun_runtime_internal.h"
+
+namespace kungpu {
+
+template <typename T>
+__global__ void fill_rect_nan(T *p, long long pitch, long long rows, long long col0, long long ncols) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * ncols) return;
+    const long long r = i / ncols, c = i % ncols;
+    p[r * pitch + col0 + c] = (T)__int_as_float(0x7fc00000);
+}
+
+__global__ void advance_tick(long long *tick, int nseg) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nseg) tick[k] += 1;
+}
+
+static size_t elem_of(const KunGpuModuleDesc *m) { return m->dtype == 0 ? 4 : 8; }
+
+bool StreamStore::alloc(const KunGpuModuleDesc *mod, long long capacity) {
+    m = mod;
+    cap = capacity;
+    size_t elem = elem_of(m);
+    rings.assign(m->num_buffers, nullptr);
+    st_t.assign(m->num_stages, nullptr);
+    st_i.assign(m->num_stages, nullptr);
+    for (int b = 0; b < m->num_buffers; b++) {
+        size_t w = (size_t)(m->buffers[b].window > 0 ? m->buffers[b].window : 1);
+        if (cudaMalloc(&rings[b], w * (size_t)cap * elem) != cudaSuccess) return false;
+    }
+    for (int s = 0; s < m->num_stages; s++) {
+        const KunGpuStageDesc &d = m->stages[s];
+        if (d.state_t_vars && cudaMalloc(&st_t[s], (size_t)d.state_t_vars * cap * elem) != cudaSuccess) return false;
+        if (d.state_i_vars && cudaMalloc(&st_i[s], (size_t)d.state_i_vars * cap * 4) != cudaSuccess) return false;
+    }
+    if (cudaMalloc(&d_init, 4 * sizeof(int64_t)) != cudaSuccess) return false;
+    return true;
+}
+
+void StreamStore::release() {
+    for (auto p : rings)
+        if (p) cudaFree(p);
+    for (auto p : st_t)
+        if (p) cudaFree(p);
+    for (auto p : st_i)
+        if (p) cudaFree(p);
+    if (d_init) cudaFree(d_init);
+    rings.clear();
+    st_t.clear();
+    st_i.clear();
+    d_init = nullptr;
+}
+
+size_t StreamStore::bytes_per_stock() const {
+    size_t elem = elem_of(m), n = 0;
+    for (int b = 0; b < m->num_buffers; b++) n += (size_t)(m->buffers[b].window > 0 ? m->buffers[b].window : 1) * elem;
+    for (int s = 0; s < m->num_stages; s++)
+        n += (size_t)m->stages[s].state_t_vars * elem + (size_t)m->stages[s].state_i_vars * 4;
+    return n;
+}
+
+// NaN-fill the ring columns of stocks [stock0, stock0 + count) and reset
+// their op states (the ops' constructors, cpp/Kun/Ops.hpp).
+KunStatus StreamStore::reset(long long stock0, long long count, cudaStream_t st) {
+    size_t elem = elem_of(m);
+    for (int b = 0; b < m->num_buffers; b++) {
+        long long w = m->buffers[b].window > 0 ? m->buffers[b].window : 1;
+        long long n = w * count;
+        unsigned grid = (unsigned)((n + 255) / 256);
+        if (elem == 4)
+            fill_rect_nan<float><<<grid, 256, 0, st>>>((float *)rings[b], cap, w, stock0, count);
+        else
+            fill_rect_nan<double><<<grid, 256, 0, st>>>((double *)rings[b], cap, w, stock0, count);
+    }
+    int32_t h_seg[3] = {0, (int32_t)count, (int32_t)stock0};
+    cudaMemcpyAsync(d_init, h_seg, sizeof h_seg, cudaMemcpyHostToDevice, st);
+    for (int s = 0; s < m->num_stages; s++) {
+        const KunGpuStageDesc &d = m->stages[s];
+        if (!d.init) continue;
+        KunGpuStageArgs a;
+        memset(&a, 0, sizeof a);
+        a.buffers = rings.data();
+        a.num_stocks = cap;
+        a.state = st_t[s];
+        a.state_i = st_i[s];
+        a.seg_off = (const int32_t *)d_init;
+        a.seg_stock0 = (const int32_t *)d_init + 2;
+        a.nseg = 1;
+        a.n_active = count;
+        int rc = d.init(&a, (void *)st);
+        if (rc) {
+            set_error("state init of stage %d failed: %s", s, cudaGetErrorString((cudaError_t)rc));
+            return KUN_CUDA_ERROR;
+        }
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        set_error("CUDA error: %s", cudaGetErrorString(e));
+        return KUN_CUDA_ERROR;
+    }
+    return KUN_SUCCESS;
+}
+
+// Enqueue one tick of every stage for the segments in d_seg / d_tick.
+KunStatus enqueue_tick(const StreamStore &store, const std::vector<int> &order, const int32_t *d_seg_off,
+                       const int32_t *d_seg_stock0, const int64_t *d_tick, int nseg, long long n_active,
+                       int max_len, cudaStream_t st) {
+    const KunGpuModuleDesc *m = store.m;
+    for (int si : order) {
+        const KunGpuStageDesc &d = m->stages[si];
+        KunGpuStageArgs a;
+        memset(&a, 0, sizeof a);
+        a.buffers = store.rings.data();
+        a.num_stocks = store.cap;
+        a.total_time = 1;
+        a.length = 1;
+        a.state = store.st_t[si];
+        a.state_i = store.st_i[si];
+        a.seg_off = d_seg_off;
+        a.seg_stock0 = d_seg_stock0;
+        a.seg_tick = d_tick;
+        a.nseg = nseg;
+        a.n_active = n_active;
+        a.max_seg_len = max_len;
+        int rc = d.launch(&a, (void *)st);
+        if (rc) {
+            set_error("stage %d (%s) failed: %s", si, d.name, cudaGetErrorString((cudaError_t)rc));
+            return KUN_CUDA_ERROR;
+        }
+    }
+    return KUN_SUCCESS;
+}
+
+bool stream_order(const KunGpuModuleDesc *m, std::vector<int> &order) {
+    std::vector<int> pending(m->num_stages);
+    for (int i = 0; i < m->num_stages; i++) pending[i] = m->stages[i].pending;
+    std::vector<int> ready;
+    for (int i = 0; i < m->num_stages; i++)
+        if (pending[i] == 0) ready.push_back(i);
+    size_t head = 0;
+    while (head < ready.size()) {
+        int i = ready[head++];
+        order.push_back(i);
+        for (int d = 0; d < m->stages[i].num_deps; d++) {
+            int j = m->stages[i].deps[d];
+            if (j >= 0 && --pending[j] == 0) ready.push_back(j);
+        }
+    }
+    return (int)order.size() == m->num_stages;
+}
+
+struct StreamCtx {
+    Executor *ex = nullptr;
+    const KunGpuModuleDesc *m = nullptr;
+    long long S = 0;
+    long long tick = 0;
+    StreamStore store;
+    std::vector<int> order;
+    int32_t *d_seg = nullptr;  // seg_off[2], seg_stock0[1]
+    int64_t *d_tick = nullptr;
+    std::vector<int> last_row;
+    std::vector<std::vector<char>> mirror;
+    cudaGraphExec_t graph = nullptr;
+    cudaStream_t stream() const { return ex->streams[0]; }
+    ~StreamCtx() {
+        if (graph) cudaGraphExecDestroy(graph);
+        if (d_seg) cudaFree(d_seg);
+        if (d_tick) cudaFree(d_tick);
+        store.release();
+    }
+};
+
+static int win_of(const KunGpuModuleDesc *m, int b) { return m->buffers[b].window > 0 ? m->buffers[b].window : 1; }
+
+static KunStatus build_graph(StreamCtx *c) {
+    cudaStream_t st = c->stream();
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        set_error("cannot capture the tick graph");
+        return KUN_CUDA_ERROR;
+    }
+    KunStatus rs = enqueue_tick(c->store, c->order, c->d_seg, c->d_seg + 2, c->d_tick, 1, c->S, (int)c->S, st);
+    advance_tick<<<1, 32, 0, st>>>((long long *)c->d_tick, 1);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rs != KUN_SUCCESS || e != cudaSuccess || !g) {
+        if (g) cudaGraphDestroy(g);
+        if (rs == KUN_SUCCESS) set_error("tick graph capture failed: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return rs == KUN_SUCCESS ? KUN_CUDA_ERROR : rs;
+    }
+    e = cudaGraphInstantiate(&c->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        set_error("tick graph instantiate failed: %s", cudaGetErrorString(e));
+        return KUN_CUDA_ERROR;
+    }
+    return KUN_SUCCESS;
+}
+
+// ------------------------------------------------------------ serialisation
+// Own format (the reference's is explicitly non-portable, doc/Stream.md):
+//   "KUNGPUS1" | u32 version | u32 dtype | i64 stocks | i64 tick |
+//   u32 buffers | u32 stages | char[64] module name |
+//   per buffer: i32 window, i32 last row, window x stocks values |
+//   per stage: i32 float vars, i32 int vars, the arrays (stocks columns).
+static const char kMagic[8] = {'K', 'U', 'N', 'G', 'P', 'U', 'S', '1'};
+
+struct Writer {
+    virtual bool write(const void *p, size_t n) = 0;
+    virtual ~Writer() = default;
+};
+struct MemWriter : Writer {
+    char *buf;
+    size_t cap, pos = 0;
+    MemWriter(char *b, size_t c) : buf(b), cap(c) {}
+    bool write(const void *p, size_t n) override {
+        if (buf && pos + n <= cap) memcpy(buf + pos, p, n);
+        pos += n;
+        return true;
+    }
+};
+struct FileWriter : Writer {
+    std::ofstream f;
+    explicit FileWriter(const char *path) : f(path, std::ios::binary) {}
+    bool write(const void *p, size_t n) override {
+        f.write((const char *)p, (std::streamsize)n);
+        return (bool)f;
+    }
+};
+struct Reader {
+    virtual bool read(void *p, size_t n) = 0;
+    virtual ~Reader() = default;
+};
+struct MemReader : Reader {
+    const char *buf;
+    size_t size, pos = 0;
+    MemReader(const char *b, size_t s) : buf(b), size(s) {}
+    bool read(void *p, size_t n) override {
+        if (pos + n > size) return false;
+        memcpy(p, buf + pos, n);
+        pos += n;
+        return true;
+    }
+};
+struct FileReader : Reader {
+    std::ifstream f;
+    explicit FileReader(const char *path) : f(path, std::ios::binary) {}
+    bool read(void *p, size_t n) override {
+        f.read((char *)p, (std::streamsize)n);
+        return (bool)f && (size_t)f.gcount() == n;
+    }
+};
+
+// copy rows [0, rows) x columns [col0, col0 + n) of a pitched device array
+static bool dev_to_host_cols(std::vector<char> &host, const void *dev, size_t elem, long long pitch, long long rows,
+                             long long col0, long long n, cudaStream_t st) {
+    host.resize((size_t)rows * n * elem);
+    if (!rows || !n) return true;
+    return cudaMemcpy2DAsync(host.data(), n * elem, (const char *)dev + col0 * elem, pitch * elem, n * elem, rows,
+                             cudaMemcpyDeviceToHost, st) == cudaSuccess;
+}
+static bool host_to_dev_cols(void *dev, const std::vector<char> &host, size_t elem, long long pitch, long long rows,
+                             long long col0, long long n, cudaStream_t st) {
+    if (!rows || !n) return true;
+    return cudaMemcpy2DAsync((char *)dev + col0 * elem, pitch * elem, host.data(), n * elem, n * elem, rows,
+                             cudaMemcpyHostToDevice, st) == cudaSuccess;
+}
+
+bool serialize_range(const StreamStore &store, long long col0, long long n, long long tick,
+                     const std::vector<int> &last_row, Writer &w, cudaStream_t st) {
+    const KunGpuModuleDesc *m = store.m;
+    size_t elem = elem_of(m);
+    uint32_t ver = 1, dt = (uint32_t)m->dtype, nb = (uint32_t)m->num_buffers, ns = (uint32_t)m->num_stages;
+    int64_t stocks = n, tk = tick;
+    char name[64] = {0};
+    strncpy(name, m->name, 63);
+    w.write(kMagic, 8);
+    w.write(&ver, 4);
+    w.write(&dt, 4);
+    w.write(&stocks, 8);
+    w.write(&tk, 8);
+    w.write(&nb, 4);
+    w.write(&ns, 4);
+    w.write(name, 64);
+    std::vector<char> host;
+    for (int b = 0; b < m->num_buffers; b++) {
+        int32_t win = win_of(m, b), lr = last_row[b];
+        w.write(&win, 4);
+        w.write(&lr, 4);
+        if (!dev_to_host_cols(host, store.rings[b], elem, store.cap, win, col0, n, st)) return false;
+        cudaStreamSynchronize(st);
+        if (!w.write(host.data(), host.size())) return false;
+    }
+    for (int s = 0; s < m->num_stages; s++) {
+        const KunGpuStageDesc &d = m->stages[s];
+        int32_t nt = d.state_t_vars, ni = d.state_i_vars;
+        w.write(&nt, 4);
+        w.write(&ni, 4);
+        if (nt) {
+            if (!dev_to_host_cols(host, store.st_t[s], elem, store.cap, nt, col0, n, st)) return false;
+            cudaStreamSynchronize(st);
+            if (!w.write(host.data(), host.size())) return false;
+        }
+        if (ni) {
+            if (!dev_to_host_cols(host, store.st_i[s], 4, store.cap, ni, col0, n, st)) return false;
+            cudaStreamSynchronize(st);
+            if (!w.write(host.data(), host.size())) return false;
+        }
+    }
+    return true;
+}
+
+// Restores a range; on failure sets the reference's error text.
+bool deserialize_range(StreamStore &store, long long col0, long long n, long long &tick, std::vector<int> &last_row,
+                       Reader &r, cudaStream_t st) {
+    const KunGpuModuleDesc *m = store.m;
+    size_t elem = elem_of(m);
+    char magic[8];
+    uint32_t ver, dt, nb, ns;
+    int64_t stocks, tk;
+    char name[64];
+    if (!r.read(magic, 8) || memcmp(magic, kMagic, 8) || !r.read(&ver, 4) || ver != 1 || !r.read(&dt, 4) ||
+        dt != (uint32_t)m->dtype || !r.read(&stocks, 8) || stocks != n || !r.read(&tk, 8) || !r.read(&nb, 4) ||
+        nb != (uint32_t)m->num_buffers || !r.read(&ns, 4) || ns != (uint32_t)m->num_stages || !r.read(name, 64) ||
+        strncmp(name, m->name, 63)) {
+        set_error("Failed to read initial stream buffer");
+        return false;
+    }
+    std::vector<char> host;
+    last_row.assign(m->num_buffers, 0);
+    for (int b = 0; b < m->num_buffers; b++) {
+        int32_t win, lr;
+        if (!r.read(&win, 4) || win != win_of(m, b) || !r.read(&lr, 4) || lr < 0 || lr >= win) {
+            set_error("Failed to read initial stream buffer");
+            return false;
+        }
+        last_row[b] = lr;
+        host.resize((size_t)win * n * elem);
+        if (!r.read(host.data(), host.size())) {
+            set_error("Failed to read initial stream buffer");
+            return false;
+        }
+        host_to_dev_cols(store.rings[b], host, elem, store.cap, win, col0, n, st);
+        cudaStreamSynchronize(st);
+    }
+    for (int s = 0; s < m->num_stages; s++) {
+        const KunGpuStageDesc &d = m->stages[s];
+        int32_t nt, ni;
+        if (!r.read(&nt, 4) || nt != d.state_t_vars || !r.read(&ni, 4) || ni != d.state_i_vars) {
+            set_error("Failed to deserialize state buffer");
+            return false;
+        }
+        if (nt) {
+            host.resize((size_t)nt * n * elem);
+            if (!r.read(host.data(), host.size())) {
+                set_error("Failed to deserialize state buffer");
+                return false;
+            }
+            host_to_dev_cols(store.st_t[s], host, elem, store.cap, nt, col0, n, st);
+            cudaStreamSynchronize(st);
+        }
+        if (ni) {
+            host.resize((size_t)ni * n * 4);
+            if (!r.read(host.data(), host.size())) {
+                set_error("Failed to deserialize state buffer");
+                return false;
+            }
+            host_to_dev_cols(store.st_i[s], host, 4, store.cap, ni, col0, n, st);
+            cudaStreamSynchronize(st);
+        }
+    }
+    tick = tk;
+    return true;
+}
+
+static StreamCtx *create_ctx(Executor *ex, const KunGpuModuleDesc *m, long long S, Reader *init, KunStatus &rc) {
+    rc = KUN_INVALID_ARGUMENT;
+    if (!ex || !m) {
+        set_error("null executor or module");
+        return nullptr;
+    }
+    if (m->abi != KUN_GPU_MODULE_ABI) {
+        set_error("The required version in the module does not match the runtime version");
+        return nullptr;
+    }
+    if (m->output_layout != KUN_LAYOUT_STREAM) {
+        set_error("Cannot run batch mode module via StreamContext");
+        return nullptr;
+    }
+    if (S <= 0) {
+        set_error("Bad num_stocks");
+        return nullptr;
+    }
+    cudaSetDevice(ex->device);
+    auto *c = new StreamCtx();
+    c->ex = ex;
+    c->m = m;
+    c->S = S;
+    rc = KUN_OUT_OF_MEMORY;
+    if (!stream_order(m, c->order)) {
+        set_error("module %s: cyclic stage graph", m->name);
+        rc = KUN_INVALID_ARGUMENT;
+        delete c;
+        return nullptr;
+    }
+    if (!c->store.alloc(m, S) || cudaMalloc(&c->d_seg, 3 * sizeof(int32_t)) != cudaSuccess ||
+        cudaMalloc(&c->d_tick, sizeof(int64_t)) != cudaSuccess) {
+        cudaGetLastError();
+        set_error("out of device memory for a stream of %lld stocks", S);
+        delete c;
+        return nullptr;
+    }
+    cudaStream_t st = c->stream();
+    int32_t seg[3] = {0, (int32_t)S, 0};
+    cudaMemcpyAsync(c->d_seg, seg, sizeof seg, cudaMemcpyHostToDevice, st);
+    rc = c->store.reset(0, S, st);
+    if (rc != KUN_SUCCESS) {
+        delete c;
+        return nullptr;
+    }
+    c->last_row.resize(m->num_buffers);
+    for (int b = 0; b < m->num_buffers; b++) c->last_row[b] = win_of(m, b) - 1;
+    if (init) {
+        if (!deserialize_range(c->store, 0, S, c->tick, c->last_row, *init, st)) {
+            rc = KUN_INIT_ERROR;
+            delete c;
+            return nullptr;
+        }
+    }
+    int64_t tk = c->tick;
+    cudaMemcpyAsync(c->d_tick, &tk, sizeof tk, cudaMemcpyHostToDevice, st);
+    cudaStreamSynchronize(st);
+    c->mirror.resize(m->num_buffers);
+    rc = build_graph(c);
+    if (rc != KUN_SUCCESS) {
+        delete c;
+        return nullptr;
+    }
+    rc = KUN_SUCCESS;
+    return c;
+}
+
+static KunStatus ctx_run(StreamCtx *c, bool sync) {
+    cudaStream_t st = c->stream();
+    cudaError_t e = cudaGraphLaunch(c->graph, st);
+    if (e != cudaSuccess) {
+        set_error("tick launch failed: %s", cudaGetErrorString(e));
+        return KUN_CUDA_ERROR;
+    }
+    const KunGpuModuleDesc *m = c->m;
+    for (int b = 0; b < m->num_buffers; b++)
+        if (m->buffers[b].kind != KUN_BUF_INPUT) c->last_row[b] = (int)(c->tick % win_of(m, b));
+    c->tick++;
+    if (sync) {
+        e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) {
+            set_error("CUDA error: %s", cudaGetErrorString(e));
+            return KUN_CUDA_ERROR;
+        }
+    }
+    return KUN_SUCCESS;
+}
+
+static bool valid_handle(StreamCtx *c, size_t h) {
+    if (!c || h >= (size_t)c->m->num_buffers) {
+        set_error("Bad buffer handle");
+        return false;
+    }
+    return true;
+}
+
+}  // namespace kungpu
+
+using namespace kungpu;
+
+static StreamCtx *C(KunStreamContextHandle h) { return (StreamCtx *)h; }
+
+KUN_EXPORT KunStreamContextHandle kunCreateStream(KunExecutorHandle exec, KunModuleHandle m, size_t num_stocks) {
+    clear_error();
+    KunStatus rc;
+    return create_ctx((Executor *)exec, (const KunGpuModuleDesc *)m, (long long)num_stocks, nullptr, rc);
+}
+
+KUN_EXPORT KunStatus kunCreateStreamEx(KunExecutorHandle exec, KunModuleHandle m, size_t num_stocks,
+                                       const KunStreamExtraArgs *extra, KunStreamContextHandle *out) {
+    clear_error();
+    if (out) *out = nullptr;
+    if (!out) return KUN_INVALID_ARGUMENT;
+    std::unique_ptr<Reader> reader;
+    if (extra) {
+        if (extra->version != KUN_API_VERSION) return KUN_INVALID_ARGUMENT;
+        if (extra->init_kind == KUN_INIT_FILE) {
+            if (!extra->init.path) return KUN_INVALID_ARGUMENT;
+            reader.reset(new FileReader(extra->init.path));
+        } else if (extra->init_kind == KUN_INIT_MEMORY) {
+            if (!extra->init.memory.buffer) return KUN_INVALID_ARGUMENT;
+            reader.reset(new MemReader(extra->init.memory.buffer, extra->init.memory.size));
+        } else if (extra->init_kind != KUN_INIT_NONE) {
+            return KUN_INVALID_ARGUMENT;
+        }
+    }
+    KunStatus rc;
+    StreamCtx *c = create_ctx((Executor *)exec, (const KunGpuModuleDesc *)m, (long long)num_stocks, reader.get(), rc);
+    if (!c) return rc == KUN_SUCCESS ? KUN_INIT_ERROR : rc;
+    *out = c;
+    return KUN_SUCCESS;
+}
+
+KUN_EXPORT KunStatus kunStreamSerializeStates(KunStreamContextHandle context, KunStateBufferKind kind,
+                                              char *path_or_buffer, size_t *size) {
+    StreamCtx *c = C(context);
+    if (!c) return KUN_INVALID_ARGUMENT;
+    cudaStream_t st = c->stream();
+    cudaStreamSynchronize(st);
+    if (kind == KUN_INIT_FILE) {
+        if (!path_or_buffer) return KUN_INVALID_ARGUMENT;
+        FileWriter w(path_or_buffer);
+        return serialize_range(c->store, 0, c->S, c->tick, c->last_row, w, st) ? KUN_SUCCESS : KUN_INIT_ERROR;
+    }
+    if (kind == KUN_INIT_MEMORY) {
+        // two-phase size query as the reference (cpp/Kun/CApi.cpp:139-164)
+        if (!size || (*size != 0 && !path_or_buffer)) return KUN_INVALID_ARGUMENT;
+        size_t in = *size;
+        MemWriter w(in ? path_or_buffer : nullptr, in);
+        if (!serialize_range(c->store, 0, c->S, c->tick, c->last_row, w, st)) return KUN_INVALID_ARGUMENT;
+        *size = w.pos;
+        return w.pos > in ? KUN_INIT_ERROR : KUN_SUCCESS;
+    }
+    return KUN_INVALID_ARGUMENT;
+}
+
+KUN_EXPORT size_t kunQueryBufferHandle(KunStreamContextHandle context, const char *name) {
+    StreamCtx *c = C(context);
+    if (!c || !name) return (size_t)-1;
+    for (int b = 0; b < c->m->num_buffers; b++)
+        if (!strcmp(c->m->buffers[b].name, name)) return (size_t)b;
+    set_error("Cannot find the buffer name");
+    return (size_t)-1;
+}
+
+KUN_EXPORT const void *kunStreamGetCurrentBufferDevice(KunStreamContextHandle context, size_t h) {
+    StreamCtx *c = C(context);
+    if (!valid_handle(c, h)) return nullptr;
+    size_t elem = elem_of(c->m);
+    return (const char *)c->store.rings[h] + (size_t)c->last_row[h] * c->S * elem;
+}
+
+KUN_EXPORT const float *kunStreamGetCurrentBuffer(KunStreamContextHandle context, size_t h) {
+    StreamCtx *c = C(context);
+    if (!valid_handle(c, h)) return nullptr;
+    size_t elem = elem_of(c->m);
+    auto &mir = c->mirror[h];
+    mir.resize((size_t)c->S * elem);
+    cudaMemcpyAsync(mir.data(), kunStreamGetCurrentBufferDevice(context, h), mir.size(), cudaMemcpyDeviceToHost,
+                    c->stream());
+    if (cudaStreamSynchronize(c->stream()) != cudaSuccess) {
+        set_error("CUDA error reading a stream buffer");
+        return nullptr;
+    }
+    return (const float *)mir.data();
+}
+
+static KunStatus push(StreamCtx *c, size_t h, const void *src, cudaMemcpyKind kind) {
+    if (!valid_handle(c, h) || !src) return KUN_INVALID_ARGUMENT;
+    size_t elem = elem_of(c->m);
+    int row = (int)(c->tick % win_of(c->m, (int)h));
+    cudaError_t e = cudaMemcpyAsync((char *)c->store.rings[h] + (size_t)row * c->S * elem, src, (size_t)c->S * elem,
+                                    kind, c->stream());
+    if (e != cudaSuccess) {
+        set_error("push failed: %s", cudaGetErrorString(e));
+        return KUN_CUDA_ERROR;
+    }
+    c->last_row[h] = row;
+    return KUN_SUCCESS;
+}
+
+KUN_EXPORT void kunStreamPushData(KunStreamContextHandle context, size_t h, const float *buffer) {
+    push(C(context), h, buffer, cudaMemcpyDefault);
+}
+
+KUN_EXPORT KunStatus kunStreamPushDataDevice(KunStreamContextHandle context, size_t h, const void *device_buffer) {
+    return push(C(context), h, device_buffer, cudaMemcpyDeviceToDevice);
+}
+
+KUN_EXPORT void kunStreamRun(KunStreamContextHandle context) {
+    if (C(context)) ctx_run(C(context), true);
+}
+
+KUN_EXPORT KunStatus kunStreamRunEx(KunStreamContextHandle context, int synchronize) {
+    if (!C(context)) return KUN_INVALID_ARGUMENT;
+    return ctx_run(C(context), synchronize != 0);
+}
+
+KUN_EXPORT void kunDestoryStream(KunStreamContextHandle context) {
+    StreamCtx *c = C(context);
+    if (!c) return;
+    cudaStreamSynchronize(c->stream());
+    delete c;
+}
+
+// GPU extension: the number of ticks the stream has run.
+KUN_EXPORT int64_t kunStreamTick(KunStreamContextHandle context) { return C(context) ? C(context)->tick : -1; }
+
+// GPU extension: device bytes one stock of this stream module occupies.
+KUN_EXPORT int64_t kunStreamBytesPerStock(KunModuleHandle m) {
+    StreamStore s;
+    s.m = (const KunGpuModuleDesc *)m;
+    return (int64_t)s.bytes_per_stock();
+}
+
+// GPU extension: copy the current row of a buffer to device memory `dst`
+// (num_stocks values), ordered after the stream's queued ticks.
+KUN_EXPORT KunStatus kunStreamCopyCurrentDevice(KunStreamContextHandle context, size_t h, void *dst) {
+    StreamCtx *c = C(context);
+    if (!valid_handle(c, h) || !dst) return KUN_INVALID_ARGUMENT;
+    size_t elem = elem_of(c->m);
+    cudaError_t e = cudaMemcpyAsync(dst, kunStreamGetCurrentBufferDevice(context, h), (size_t)c->S * elem,
+                                    cudaMemcpyDeviceToDevice, c->stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream());
+    if (e != cudaSuccess) {
+        set_error("CUDA error: %s", cudaGetErrorString(e));
+        return KUN_CUDA_ERROR;
+    }
+    return KUN_SUCCESS;
+}

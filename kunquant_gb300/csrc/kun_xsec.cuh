@@ -42,65 +42,84 @@ template <> struct SortKey<double> {
 
 constexpr int kRankThreads = 1024;
 
+// Rank of one row by the whole block: keys[P] and cnt_warp are shared memory.
+template <typename T>
+__device__ __forceinline__ void rank_one_row(const T *__restrict__ row, T *__restrict__ orow, long long S, int P,
+                                             typename SortKey<T>::K *keys, int *cnt_warp) {
+    using SK = SortKey<T>;
+    using K = typename SK::K;
+    const int tid = threadIdx.x;
+    int local = 0;
+    for (int i = tid; i < P; i += blockDim.x) {
+        K k = SK::kMax;
+        if (i < S) {
+            T x = row[i];
+            k = SK::enc(x);
+            local += (x == x);
+        }
+        keys[i] = k;
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((tid & 31) == 0) cnt_warp[tid >> 5] = local;
+    __syncthreads();
+    int n = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) n += cnt_warp[w];
+    for (int k = 2; k <= P; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = tid; i < P; i += blockDim.x) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    K a = keys[i], b = keys[ixj];
+                    bool up = (i & k) == 0;
+                    if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    for (int i = tid; i < S; i += blockDim.x) {
+        T x = row[i];
+        T r;
+        if (x != x) {
+            r = knan<T>();
+        } else {
+            int lo = 0, hi = n;
+            while (lo < hi) { int m = (lo + hi) >> 1; if (SK::dec(keys[m]) < x) lo = m + 1; else hi = m; }
+            long long start = lo;
+            hi = n;
+            while (lo < hi) { int m = (lo + hi) >> 1; if (x < SK::dec(keys[m])) hi = m; else lo = m + 1; }
+            long long end = lo;
+            long long sum = (start + end + 1) * (end - start) / 2;
+            r = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
+        }
+        orow[i] = r;
+    }
+    __syncthreads();
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ in, T *__restrict__ out,
                                                           long long S, long long length, int P) {
-    using SK = SortKey<T>;
-    using K = typename SK::K;
+    using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    K *keys = reinterpret_cast<K *>(smem_raw);
     __shared__ int cnt_warp[kRankThreads / 32];
-    const int tid = threadIdx.x;
-    for (long long t = blockIdx.x; t < length; t += gridDim.x) {
-        const T *row = in + t * S;
-        T *orow = out + t * S;
-        int local = 0;
-        for (int i = tid; i < P; i += blockDim.x) {
-            K k = SK::kMax;
-            if (i < S) {
-                T x = row[i];
-                k = SK::enc(x);
-                local += (x == x);
-            }
-            keys[i] = k;
-        }
-        for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-        if ((tid & 31) == 0) cnt_warp[tid >> 5] = local;
-        __syncthreads();
-        int n = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) n += cnt_warp[w];
-        for (int k = 2; k <= P; k <<= 1) {
-            for (int j = k >> 1; j > 0; j >>= 1) {
-                for (int i = tid; i < P; i += blockDim.x) {
-                    int ixj = i ^ j;
-                    if (ixj > i) {
-                        K a = keys[i], b = keys[ixj];
-                        bool up = (i & k) == 0;
-                        if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
-                    }
-                }
-                __syncthreads();
-            }
-        }
-        for (int i = tid; i < S; i += blockDim.x) {
-            T x = row[i];
-            T r;
-            if (x != x) {
-                r = knan<T>();
-            } else {
-                int lo = 0, hi = n;
-                while (lo < hi) { int m = (lo + hi) >> 1; if (SK::dec(keys[m]) < x) lo = m + 1; else hi = m; }
-                long long start = lo;
-                hi = n;
-                while (lo < hi) { int m = (lo + hi) >> 1; if (x < SK::dec(keys[m])) hi = m; else lo = m + 1; }
-                long long end = lo;
-                long long sum = (start + end + 1) * (end - start) / 2;
-                r = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
-            }
-            orow[i] = r;
-        }
-        __syncthreads();
-    }
+    for (long long t = blockIdx.x; t < length; t += gridDim.x)
+        rank_one_row<T>(in + t * S, out + t * S, S, P, reinterpret_cast<K *>(smem_raw), cnt_warp);
+}
+
+// stream mode: one block per segment, each at its own ring row
+template <typename T>
+__global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restrict__ in, int w_in, T *__restrict__ out,
+                                                              int w_out, long long cap, const int32_t *seg_off,
+                                                              const int32_t *seg_stock0, const long long *seg_tick,
+                                                              int P) {
+    using K = typename SortKey<T>::K;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int cnt_warp[kRankThreads / 32];
+    const int k = blockIdx.x;
+    const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
+    rank_one_row<T>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, P,
+                    reinterpret_cast<K *>(smem_raw), cnt_warp);
 }
 
 template <typename T>
@@ -148,6 +167,51 @@ __global__ void __launch_bounds__(256) diffwsum_rows(const T *__restrict__ in0, 
     }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(256) scale_segments(const T *__restrict__ in, int w_in, T *__restrict__ out,
+                                                      int w_out, long long cap, const int32_t *seg_off,
+                                                      const int32_t *seg_stock0, const long long *seg_tick) {
+    __shared__ T total;
+    const int k = blockIdx.x;
+    const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
+    const T *row = in + (n % w_in) * cap + s0;
+    T *orow = out + (n % w_out) * cap + s0;
+    if (threadIdx.x == 0) {
+        T sum = 0;
+        for (long long i = 0; i < len; i++) {
+            T x = row[i];
+            if (x == x) sum = kadd(sum, kabs(x));
+        }
+        total = sum;
+    }
+    __syncthreads();
+    const T sum = total;
+    for (long long i = threadIdx.x; i < len; i += blockDim.x) {
+        T x = row[i];
+        orow[i] = (x == T(0) && sum == T(0)) ? knan<T>() : kdiv(x, sum);
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) diffwsum_segments(const T *__restrict__ in0, int w0, const T *__restrict__ in1,
+                                                         int w1, T *__restrict__ out, int w_out, long long cap,
+                                                         const int32_t *seg_off, const int32_t *seg_stock0,
+                                                         const long long *seg_tick) {
+    __shared__ T total;
+    const int k = blockIdx.x;
+    const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
+    const T *a = in0 + (n % w0) * cap + s0, *b = in1 + (n % w1) * cap + s0;
+    T *orow = out + (n % w_out) * cap + s0;
+    if (threadIdx.x == 0) {
+        T sum = 0;
+        for (long long i = 0; i < len; i++) sum = kadd(sum, kmul(a[i], b[i]));
+        total = sum;
+    }
+    __syncthreads();
+    const T sum = total;
+    for (long long i = threadIdx.x; i < len; i += blockDim.x) orow[i] = ksub(a[i], sum);
+}
+
 inline int kun_num_sms() {
     static int n = 0;
     if (!n) {
@@ -192,6 +256,43 @@ template <typename T>
 inline int launch_diffwsum(const T *in0, const T *in1, T *out, long long S, long long length, cudaStream_t st) {
     long long grid = length < (long long)kun_num_sms() * 4 ? length : (long long)kun_num_sms() * 4;
     diffwsum_rows<T><<<(unsigned)grid, 256, 0, st>>>(in0, in1, out, S, length);
+    return (int)cudaGetLastError();
+}
+
+template <typename T>
+inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long long cap, const int32_t *seg_off,
+                                const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
+                                cudaStream_t st) {
+    using K = typename SortKey<T>::K;
+    int P = 1;
+    while (P < max_len) P <<= 1;
+    size_t smem = (size_t)P * sizeof(K);
+    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(rank_segments<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    rank_segments<T><<<(unsigned)nseg, kRankThreads, smem, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0,
+                                                                 seg_tick, P);
+    return (int)cudaGetLastError();
+}
+
+template <typename T>
+inline int launch_scale_segments(const T *in, int w_in, T *out, int w_out, long long cap, const int32_t *seg_off,
+                                 const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
+                                 cudaStream_t st) {
+    (void)max_len;
+    scale_segments<T><<<(unsigned)nseg, 256, 0, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0, seg_tick);
+    return (int)cudaGetLastError();
+}
+
+template <typename T>
+inline int launch_diffwsum_segments(const T *in0, int w0, const T *in1, int w1, T *out, int w_out, long long cap,
+                                    const int32_t *seg_off, const int32_t *seg_stock0, const long long *seg_tick,
+                                    int nseg, int max_len, cudaStream_t st) {
+    (void)max_len;
+    diffwsum_segments<T><<<(unsigned)nseg, 256, 0, st>>>(in0, w0, in1, w1, out, w_out, cap, seg_off, seg_stock0,
+                                                         seg_tick);
     return (int)cudaGetLastError();
 }
 

@@ -77,6 +77,9 @@ def _load_runtime():
             "kunStreamPushDataDevice": (i32, [vp, sz, vp]),
             "kunStreamGetCurrentBufferDevice": (vp, [vp, sz]),
             "kunStreamRunEx": (i32, [vp, i32]),
+            "kunStreamCopyCurrentDevice": (i32, [vp, sz, vp]),
+            "kunStreamTick": (i64, [vp]),
+            "kunStreamBytesPerStock": (i64, [vp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -327,3 +330,146 @@ def runGraph(exec: Executor, mod: Module, inputs: dict, cur_time: int, length: i
     finally:
         L.kunDestoryBufferNameMap(m)
     return ret
+
+
+class _InitUnion(ctypes.Union):
+    class _Mem(ctypes.Structure):
+        _fields_ = [("buffer", ctypes.c_void_p), ("size", ctypes.c_size_t)]
+    _fields_ = [("path", ctypes.c_char_p), ("memory", _Mem)]
+
+
+class _StreamExtraArgs(ctypes.Structure):
+    _fields_ = [("version", ctypes.c_size_t), ("init_kind", ctypes.c_int), ("init", _InitUnion)]
+
+
+_KUN_INIT_NONE, _KUN_INIT_FILE, _KUN_INIT_MEMORY = 0, 1, 2
+
+
+class StreamContext:
+    """One stream session (``cpp/Python/PyBinding.cpp:508-596``): per tick,
+    ``pushData`` one row of every input, ``run`` and read the outputs with
+    ``getCurrentBuffer``.  ``init`` restores a ``serializeStates`` dump (a
+    file name or bytes).  Numpy rows go through host memory; torch CUDA rows
+    are pushed device to device (``pushData``) and ``getCurrentBufferDevice``
+    returns the output row as a torch tensor without a copy to the host."""
+
+    def __init__(self, exec: Executor, mod: Module, num_stocks: int, init=None):
+        if mod.output_layout != "STREAM":
+            raise KunError("Cannot run batch mode module via StreamContext")
+        L = runtime()
+        self._exec, self._mod, self.num_stocks = exec, mod, int(num_stocks)
+        self.handle = None
+        out = ctypes.c_void_p()
+        if init is None:
+            rc = L.kunCreateStreamEx(exec.handle, mod.handle, self.num_stocks, None, ctypes.byref(out))
+        else:
+            extra = _StreamExtraArgs()
+            extra.version = 1
+            if isinstance(init, str):
+                extra.init_kind = _KUN_INIT_FILE
+                path = os.fsencode(init)
+                extra.init.path = path
+            elif isinstance(init, (bytes, bytearray)):
+                extra.init_kind = _KUN_INIT_MEMORY
+                data = ctypes.create_string_buffer(bytes(init), len(init))
+                extra.init.memory.buffer = ctypes.cast(data, ctypes.c_void_p)
+                extra.init.memory.size = len(init)
+            else:
+                raise KunError("Bad type for init, expecting filename or bytes")
+            rc = L.kunCreateStreamEx(exec.handle, mod.handle, self.num_stocks, ctypes.byref(extra),
+                                     ctypes.byref(out))
+        _check(rc)
+        self.handle = out.value
+        self._rows = {}
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.kunDestoryStream(self.handle)
+            self.handle = None
+
+    def queryBufferHandle(self, name: str) -> int:
+        h = runtime().kunQueryBufferHandle(self.handle, name.encode())
+        if h == ctypes.c_size_t(-1).value:
+            raise KunError("Cannot find the buffer name")
+        return h
+
+    def _check_handle(self, handle):
+        if not (0 <= handle < self._mod.num_buffers):
+            raise KunError("Bad buffer handle")
+
+    def pushData(self, handle: int, data):
+        self._check_handle(handle)
+        dtype = self._mod.dtype
+        if _is_torch_cuda(data):
+            import torch
+            want = torch.float32 if dtype == np.float32 else torch.float64
+            if data.dtype != want or not data.is_contiguous():
+                raise KunError("Bad input type to push, expecting float")
+            if data.dim() != 1 or data.shape[0] != self.num_stocks:
+                raise KunError("Bad dimension for input data to push")
+            L = runtime()
+            # order the device copy after torch's producer of `data`
+            torch.cuda.current_stream().synchronize()
+            _check(L.kunStreamPushDataDevice(self.handle, handle, ctypes.c_void_p(data.data_ptr())))
+            return
+        if not isinstance(data, np.ndarray) or data.dtype != dtype or not data.flags["C_CONTIGUOUS"]:
+            raise KunError("Bad input type to push, expecting float")
+        if data.ndim != 1 or data.shape[0] != self.num_stocks:
+            raise KunError("Bad dimension for input data to push")
+        runtime().kunStreamPushData(self.handle, handle, data.ctypes.data_as(ctypes.c_void_p))
+
+    def run(self, synchronize: bool = True):
+        _check(runtime().kunStreamRunEx(self.handle, 1 if synchronize else 0))
+
+    def getCurrentBuffer(self, handle: int) -> np.ndarray:
+        """The current row of a buffer, copied to the host (a fresh array)."""
+        self._check_handle(handle)
+        p = runtime().kunStreamGetCurrentBuffer(self.handle, handle)
+        if not p:
+            raise KunError(_err())
+        ct = ctypes.c_float if self._mod.dtype == np.float32 else ctypes.c_double
+        arr = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ct)), shape=(self.num_stocks,))
+        return arr.copy()
+
+    def getCurrentBufferDevice(self, handle: int):
+        """The current row of a buffer as a torch CUDA tensor (a copy made on
+        the device, valid after later ticks)."""
+        import torch
+        self._check_handle(handle)
+        L = runtime()
+        p = L.kunStreamGetCurrentBufferDevice(self.handle, handle)
+        if not p:
+            raise KunError(_err())
+        dt = torch.float32 if self._mod.dtype == np.float32 else torch.float64
+        out = torch.empty(self.num_stocks, dtype=dt, device="cuda")
+        _check(L.kunStreamCopyCurrentDevice(self.handle, handle, ctypes.c_void_p(out.data_ptr())))
+        return out
+
+    def tick(self) -> int:
+        return runtime().kunStreamTick(self.handle)
+
+    def serializeStates(self, fileNameOrNone=None):
+        L = runtime()
+        if isinstance(fileNameOrNone, str):
+            n = ctypes.c_size_t(0)
+            path = ctypes.create_string_buffer(os.fsencode(fileNameOrNone))
+            rc = L.kunStreamSerializeStates(self.handle, _KUN_INIT_FILE, ctypes.cast(path, ctypes.c_void_p),
+                                            ctypes.byref(n))
+            if rc != 0:
+                raise KunError("Failed to serialize states")
+            return None
+        n = ctypes.c_size_t(0)
+        rc = L.kunStreamSerializeStates(self.handle, _KUN_INIT_MEMORY, None, ctypes.byref(n))
+        if rc not in (0, 1):
+            raise KunError("Failed to serialize states")
+        buf = ctypes.create_string_buffer(n.value)
+        rc = L.kunStreamSerializeStates(self.handle, _KUN_INIT_MEMORY, ctypes.cast(buf, ctypes.c_void_p),
+                                        ctypes.byref(n))
+        if rc != 0:
+            raise KunError("Failed to serialize states")
+        return buf.raw[:n.value]
+
+
+def streamBytesPerStock(mod: Module) -> int:
+    """Device bytes one stock of a stream module occupies (rings + states)."""
+    return int(runtime().kunStreamBytesPerStock(mod.handle))

@@ -72,6 +72,11 @@ def run_batch(key: str, inputs: dict, cur_time=0, length=None, threads=1):
 def run_stream(key: str, inputs: dict, num_ticks=None):
     """Drive the reference StreamContext tick by tick; returns {name: [T][S]}."""
     lib, mod = compile_predefined(key)
+    return run_stream_module(mod, inputs, num_ticks)
+
+
+def run_stream_module(mod, inputs: dict, num_ticks=None):
+    """run_stream for a module compiled by compile_function."""
     from KunQuant.runner import KunRunner as kr
     T, S = next(iter(inputs.values())).shape
     num_ticks = num_ticks or T

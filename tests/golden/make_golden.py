@@ -105,8 +105,34 @@ def _graphs():
         Output(Scale(a - 0.5), "scale")
         Output(DiffWithWeightedSum(a, b), "diffw")
 
+    def stream_unit():
+        # the graph of the reference's tests/test_stream.py
+        a = Input("a")
+        Output(WindowedQuantile(a, 10, 0.49), "quantile")
+        Output(ExpMovingAvg(a, 10), "ema")
+        Output(WindowedLinearRegressionSlope(a, 10), "slope")
+
+    def stream_misc():
+        a, b = Input("a"), Input("b")
+        Output(WindowedAvg(a, 10), "avg")
+        Output(WindowedStddev(a, 10), "std")
+        Output(WindowedCorrelation(a, 10, b), "corr")
+        Output(TsArgMin(a, 7), "argmin")
+        Output(TsRank(a, 9), "tsrank")
+        Output(WindowedMax(a, 6), "max")
+        Output(DecayLinear(a, 7), "decay")
+        Output(WindowedSkew(a, 12), "skew")
+        Output(WindowedKurt(a, 12), "kurt")
+        Output(Rank(a), "rank")
+        Output(Rank(WindowedSum(a, 5) - b), "rank_sum")
+        Output(Scale(a - 0.5), "scale")
+
     return {
         # name: (builder, config kwargs, input maker)
+        "stream_unit_f64": (mk(stream_unit), dict(dtype="double", input_layout="STREAM",
+                                                  output_layout="STREAM"), "stream24"),
+        "stream_misc_f32": (mk(stream_misc), dict(input_layout="STREAM", output_layout="STREAM"),
+                            "stream_ab"),
         "argmin_issue19": (mk(argmin), dict(input_layout="TS", output_layout="TS"), "issue19"),
         "rank_ties_nan": (mk(rank), dict(input_layout="TS", output_layout="TS"), "rank"),
         "rank2_exact": (mk(rank2), dict(input_layout="TS", output_layout="TS"), "u24"),
@@ -168,6 +194,14 @@ def _inputs(kind, dtype):
         a = rng.integers(0, 40, size=(600, 8)).astype(dtype) / 4
         a[300:305, 2] = np.nan
         return {"a": a}
+    if kind == "stream24":
+        return {"a": rng.random((100, 24)).astype(dtype)}
+    if kind == "stream_ab":
+        a = rng.random((80, 24)).astype(dtype)
+        b = rng.random((80, 24)).astype(dtype)
+        a[30:33, 3] = np.nan
+        a[40, :] = 0.5
+        return {"a": a, "b": b}
     raise KeyError(kind)
 
 
@@ -224,8 +258,12 @@ def main(names):
         spec, mod = refkun.compile_function("g_" + name, build, name, **cfg)
         dt = np.float32 if spec["dtype"] == "float" else np.float64
         inputs = _inputs(kind, dt)
-        out = refkun.run_module(mod, inputs)
-        _save(name, spec, inputs, out)
+        if cfg.get("output_layout") == "STREAM":
+            out = refkun.run_stream_module(mod, inputs)
+            _save(name, spec, inputs, out, {"stream": True})
+        else:
+            out = refkun.run_module(mod, inputs)
+            _save(name, spec, inputs, out)
 
 
 if __name__ == "__main__":

@@ -24,3 +24,9 @@ def load(name):
     inputs = {k[4:]: z[k] for k in z.files if k.startswith("in__")}
     outputs = {k[5:]: z[k] for k in z.files if k.startswith("out__")}
     return spec, inputs, outputs, meta
+
+
+def is_stream(name):
+    """Stream-mode fixtures hold the reference StreamContext's outputs."""
+    with gzip.open(os.path.join(GOLDEN, name + ".json.gz"), "rb") as f:
+        return bool(json.loads(f.read()).get("stream"))

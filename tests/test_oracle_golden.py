@@ -26,7 +26,7 @@ def known_inexact(name):
     return set()
 
 
-BATCH = [n for n in G.names() if not n.endswith("stream_f32")]
+BATCH = [n for n in G.names() if not G.is_stream(n)]
 
 
 @pytest.mark.parametrize("name", BATCH)
