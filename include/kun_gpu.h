@@ -155,6 +155,21 @@ int kunModuleNumStages(KunModuleHandle m);
 KunStatus kunStreamPushDataDevice(KunStreamContextHandle context, size_t handle, const void *device_buffer);
 const void *kunStreamGetCurrentBufferDevice(KunStreamContextHandle context, size_t handle);
 KunStatus kunStreamRunEx(KunStreamContextHandle context, int synchronize);
+/* Batch run that allocates no device memory; no counterpart in the reference.
+ * For callers that cannot call cudaMalloc (an allocator-owning host process,
+ * code between allocator checkpoints): temporaries and scratch come from a
+ * static device array of KUN_NOALLOC_SCRATCH_BYTES inside libkungpu.so, and
+ * no executor is needed.  Every buffer in the map must be device memory.  The
+ * work is enqueued on `cuda_stream` (0 = legacy default stream) and the call
+ * returns without waiting.  A run whose scratch would not fit is rejected
+ * with KUN_OUT_OF_MEMORY and a message giving the bytes it needs.  The first
+ * call on each device does a one-time set-up (address lookup of the static
+ * array) and should come before any stream capture on that device.  All calls
+ * on a device share the array: calls whose GPU work overlaps race and must be
+ * ordered by the caller (one stream, or events). */
+#define KUN_NOALLOC_SCRATCH_BYTES (64u << 20)
+KunStatus kunRunGraphNoAlloc(KunModuleHandle m, KunBufferNameMapHandle buffers, size_t num_stocks,
+                             size_t total_time, size_t cur_time, size_t length, void *cuda_stream);
 /* Copy the current row of a buffer (num_stocks values) to device memory. */
 KunStatus kunStreamCopyCurrentDevice(KunStreamContextHandle context, size_t handle, void *device_dst);
 /* Ticks the stream has run (the time index of the next pushed row). */

@@ -64,7 +64,7 @@ static bool topo_order(const KunGpuModuleDesc *m, std::vector<int> &order) {
 // that last touched it is an ancestor of P in the stage DAG, so the plan is
 // safe however the streams interleave (the reference frees a temporary on its
 // last deref, cpp/Kun/Runtime.cpp:84-93).
-static bool make_plan(const KunGpuModuleDesc *m, long long S, long long length, int nstreams, Plan &p) {
+bool make_plan(const KunGpuModuleDesc *m, long long S, long long length, int nstreams, Plan &p) {
     if (!topo_order(m, p.order)) {
         set_error("module %s: cyclic stage graph", m->name);
         return false;
@@ -176,8 +176,6 @@ static bool is_device_pointer(const void *ptr) {
     }
     return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
-
-using NameMap = std::unordered_map<std::string, float *>;
 
 static size_t user_buffer_elems(const KunGpuModuleDesc *m, const KunGpuBufferDesc &b, long long S,
                                 long long total_time, long long length) {

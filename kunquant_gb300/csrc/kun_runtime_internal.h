@@ -7,6 +7,7 @@
 #include <mutex>
 #include <string>
 #include <tuple>
+#include <unordered_map>
 #include <vector>
 
 #include "kun_gpu.h"
@@ -19,6 +20,9 @@ namespace kungpu {
 void set_error(const char *fmt, ...);
 void clear_error();
 const char *last_error();
+
+// buffer name -> user pointer (kunSetBufferNameMap)
+using NameMap = std::unordered_map<std::string, float *>;
 
 struct Library {
     void *handle = nullptr;
@@ -57,6 +61,10 @@ struct Plan {
     int num_slots = 0;
     size_t slot_bytes = 0;
 };
+
+// Builds the stage order and the slot assignment of temporaries and scratch
+// for `nstreams` streams; false (with the error set) on a cyclic stage graph.
+bool make_plan(const KunGpuModuleDesc *m, long long S, long long length, int nstreams, Plan &p);
 
 // A captured CUDA graph of one run, valid for the exact buffers it was
 // captured with.
