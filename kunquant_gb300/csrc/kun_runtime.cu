@@ -198,9 +198,34 @@ static void ensure_events(std::vector<cudaEvent_t> &v, size_t n, unsigned flags)
 
 // Enqueue all stages.  Single stream: in plan order.  Several streams: each
 // stage on its assigned stream after its predecessors' completion events.
+// Device-to-host copies of host output buffers, issued on copy streams as
+// soon as the stage producing each buffer has finished, so the copies of
+// early outputs overlap the kernels of later stages.
+struct OutputCopies {
+    struct Item {
+        void *host;
+        const void *dev;
+        size_t bytes;
+    };
+    std::vector<std::vector<Item>> by_stage;  // stage -> outputs it produces
+    int next = 0;
+};
+
+static void issue_stage_copies(Executor *ex, OutputCopies &oc, int si, cudaStream_t st) {
+    auto &items = oc.by_stage[si];
+    if (items.empty()) return;
+    cudaEvent_t ev = ex->copy_ev[si];
+    cudaEventRecord(ev, st);
+    for (auto &it : items) {
+        cudaStream_t cs = ex->copy_streams[oc.next++ % ex->copy_streams.size()];
+        cudaStreamWaitEvent(cs, ev, 0);
+        cudaMemcpyAsync(it.host, it.dev, it.bytes, cudaMemcpyDeviceToHost, cs);
+    }
+}
+
 static KunStatus enqueue_stages(Executor *ex, const KunGpuModuleDesc *m, const Plan &plan, void **ptrs,
                                 long long S, long long total_time, long long cur_time, long long length,
-                                cudaStream_t origin, bool multi, int64_t &launches) {
+                                cudaStream_t origin, bool multi, int64_t &launches, OutputCopies *oc = nullptr) {
     std::vector<void *> scratch;
     int ev_idx = 0;
     if (ex->profile) {
@@ -243,6 +268,7 @@ static KunStatus enqueue_stages(Executor *ex, const KunGpuModuleDesc *m, const P
             return KUN_CUDA_ERROR;
         }
         if (ex->profile) cudaEventRecord(ex->ev[++ev_idx], st);
+        if (oc) issue_stage_copies(ex, *oc, si, st);
         if (multi) {
             cudaEventRecord(ex->done[si], st);
             last_on[plan.stream_of[si]] = si;
@@ -356,7 +382,47 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
     gkey.push_back((void *)(intptr_t)nstreams);
     KunStatus rs = KUN_SUCCESS;
     GraphEntry *ge = nullptr;
-    if (ex->use_graphs && !ex->profile) {
+    // host outputs: copy each one out as soon as its stage is done (no graph
+    // replay for such runs; the copies are not part of the captured work)
+    OutputCopies oc;
+    bool overlap = !host_out.empty() && !ex->profile;
+    if (overlap) {
+        if (ex->copy_streams.empty()) {
+            for (int k = 0; k < 4; k++) {
+                cudaStream_t cs;
+                if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) break;
+                ex->copy_streams.push_back(cs);
+            }
+            if (ex->copy_streams.empty()) {
+                cudaGetLastError();
+                overlap = false;
+            }
+        }
+    }
+    if (overlap) {
+        ensure_events(ex->copy_ev, m->num_stages, cudaEventDisableTiming);
+        ensure_events(ex->copy_done, ex->copy_streams.size(), cudaEventDisableTiming);
+        oc.by_stage.assign(m->num_stages, {});
+        std::vector<int> producer(m->num_buffers, -1);
+        for (int si = 0; si < m->num_stages; si++)
+            for (int k = 0; k < m->stages[si].num_out; k++) producer[m->stages[si].out_bufs[k]] = si;
+        for (auto &hc : host_out) {
+            if (producer[hc.buf] < 0) {
+                overlap = false;
+                break;
+            }
+            oc.by_stage[producer[hc.buf]].push_back({hc.host, ptrs[hc.buf], hc.bytes});
+        }
+    }
+    if (overlap) {
+        rs = enqueue_stages(ex, m, plan, ptrs.data(), S, total_time, cur_time, length, st, multi, launches, &oc);
+        if (rs != KUN_SUCCESS) return rs;
+        for (size_t k = 0; k < ex->copy_streams.size(); k++) {
+            cudaEventRecord(ex->copy_done[k], ex->copy_streams[k]);
+            cudaStreamWaitEvent(st, ex->copy_done[k], 0);
+        }
+        host_out.clear();
+    } else if (ex->use_graphs && !ex->profile) {
         for (auto &g : ex->graphs)
             if (g.key == gkey) ge = &g;
         if (!ge && ++ex->seen[gkey] >= 2) {
@@ -390,7 +456,9 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
             }
         }
     }
-    if (ge) {
+    if (overlap) {
+        // stages and copies are enqueued
+    } else if (ge) {
         cudaError_t e = cudaGraphLaunch(ge->exec, st);
         if (e != cudaSuccess) {
             set_error("graph launch failed: %s", cudaGetErrorString(e));
@@ -402,12 +470,13 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
         if (rs != KUN_SUCCESS) return rs;
     }
     ex->last_launches = launches;
+    bool had_host_out = overlap || !host_out.empty();
     for (auto &hc : host_out) cudaMemcpyAsync(hc.host, ptrs[hc.buf], hc.bytes, cudaMemcpyDeviceToHost, st);
     if (ex->has_user_stream) {
         cudaEventRecord(ex->bridge_out, st);
         cudaStreamWaitEvent(ex->user_stream, ex->bridge_out, 0);
     }
-    if (sync || !host_in.empty() || !host_out.empty()) {
+    if (sync || !host_in.empty() || had_host_out) {
         cudaError_t e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) {
             set_error("CUDA error: %s", cudaGetErrorString(e));
@@ -449,6 +518,12 @@ void destroy_executor(Executor *ex) {
     if (ex->bridge_in) cudaEventDestroy(ex->bridge_in);
     if (ex->bridge_out) cudaEventDestroy(ex->bridge_out);
     if (ex->d_error) cudaFree(ex->d_error);
+    for (auto cs : ex->copy_streams) {
+        cudaStreamSynchronize(cs);
+        cudaStreamDestroy(cs);
+    }
+    for (auto e : ex->copy_ev) cudaEventDestroy(e);
+    for (auto e : ex->copy_done) cudaEventDestroy(e);
     delete ex;
 }
 

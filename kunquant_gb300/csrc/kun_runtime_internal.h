@@ -99,6 +99,10 @@ struct Executor {
     // bridged to the caller's stream with these events
     bool has_user_stream = false;
     cudaEvent_t bridge_in = nullptr, bridge_out = nullptr;
+    // copy streams for device-to-host output copies overlapping the stages
+    std::vector<cudaStream_t> copy_streams;
+    std::vector<cudaEvent_t> copy_ev;    // per stage: its outputs are ready
+    std::vector<cudaEvent_t> copy_done;  // per copy stream: all copies issued so far are done
     cudaStream_t stream() const { return streams[0]; }
 };
 
