@@ -7,7 +7,8 @@
  *   - an "executor" is a CUDA execution context on the current device (one or
  *     more CUDA streams) instead of a CPU thread pool;
  *   - a "library" is a module library produced by the GPU code generator
- *     (kunquant_gb300.jit.compileit or the prebuilt Alpha101/Alpha158 ones);
+ *     (kunquant_gb300.build.build_module_library, or the prebuilt
+ *     Alpha101/Alpha158 ones);
  *   - buffers given to kunSetBufferNameMap may be host or device pointers;
  *     host buffers are copied to the device and back inside kunRunGraph;
  *   - every call reports errors through its return status and
@@ -24,6 +25,7 @@ typedef void *KunLibraryHandle;
 typedef void *KunModuleHandle;
 typedef void *KunBufferNameMapHandle;
 typedef void *KunStreamContextHandle;
+typedef void *KunServePoolHandle;
 
 #ifdef __cplusplus
 extern "C" {
@@ -176,6 +178,47 @@ KunStatus kunStreamCopyCurrentDevice(KunStreamContextHandle context, size_t hand
 int64_t kunStreamTick(KunStreamContextHandle context);
 /* Device bytes one stock of a stream module holds (rings and op states). */
 int64_t kunStreamBytesPerStock(KunModuleHandle m);
+
+/* Serving pool (GPU extension; the reference runs one StreamContext per
+ * session).  Sessions of one stream module share one device store of
+ * `capacity_stocks` columns; a session keeps a contiguous column range, with
+ * its rings and op states resident, until it is closed.  A step advances any
+ * set of sessions by one tick each in one graph launch.
+ *
+ * Step data is laid out by column: inputs [num_inputs][capacity_stocks] and
+ * outputs [num_outputs][capacity_stocks] (buffers in module order); session
+ * s reads and writes columns [kunServeSessionColumn(s), + its stocks).  With
+ * `device_inputs` / `device_outputs` NULL the pool's pinned host tables
+ * (kunServeHostInputs/Outputs) are used, otherwise they are device tables of
+ * the same layout.  Only the column span of the step's sessions is copied. */
+KunStatus kunCreateServePool(KunExecutorHandle exec, KunModuleHandle m, size_t capacity_stocks, int max_sessions,
+                             int max_session_stocks, KunServePoolHandle *out);
+void kunDestroyServePool(KunServePoolHandle pool);
+/* KUN_OUT_OF_MEMORY when no slot or no free column range fits: retry after a close */
+KunStatus kunServeOpen(KunServePoolHandle pool, size_t num_stocks, int64_t *session_id);
+KunStatus kunServeClose(KunServePoolHandle pool, int64_t session_id);
+KunStatus kunServeStep(KunServePoolHandle pool, int num_sessions, const int64_t *session_ids,
+                       const void *device_inputs, void *device_outputs);
+/* Request loop (continuous batching): after kunServeStart, clients write a
+ * session's input columns, kunServeSubmit it and kunServeWait for its tick;
+ * each step takes every session submitted so far (after `batch_window_us`),
+ * so ticks that arrive while a step is on the GPU go into the next one.  A
+ * session has at most one tick in flight.  kunServeStep is for use without
+ * the loop. */
+KunStatus kunServeStart(KunServePoolHandle pool, int batch_window_us);
+KunStatus kunServeStop(KunServePoolHandle pool);
+KunStatus kunServeSubmit(KunServePoolHandle pool, int num_sessions, const int64_t *session_ids);
+KunStatus kunServeWait(KunServePoolHandle pool, int64_t session_id, int64_t min_tick, int timeout_ms);
+int kunServeTakeLatencies(KunServePoolHandle pool, float *latency_us, int cap, int32_t *step_sizes, int step_cap,
+                          int *num_steps);
+void *kunServeHostInputs(KunServePoolHandle pool);
+void *kunServeHostOutputs(KunServePoolHandle pool);
+int64_t kunServeSessionTick(KunServePoolHandle pool, int64_t session_id);
+int64_t kunServeSessionStocks(KunServePoolHandle pool, int64_t session_id);
+int64_t kunServeSessionColumn(KunServePoolHandle pool, int64_t session_id);
+KunStatus kunServeFreeStocks(KunServePoolHandle pool, int64_t *total, int64_t *largest);
+/* device bytes of a pool of `capacity_stocks` columns (store + packed rows) */
+int64_t kunServePoolBytes(KunModuleHandle m, size_t capacity_stocks);
 
 #ifdef __cplusplus
 }

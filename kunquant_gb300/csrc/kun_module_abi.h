@@ -11,7 +11,7 @@
 extern "C" {
 #endif
 
-#define KUN_GPU_MODULE_ABI 0x6b470004ull
+#define KUN_GPU_MODULE_ABI 0x6b470005ull
 
 typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
 typedef enum { KUN_BUF_INPUT = 0, KUN_BUF_OUTPUT = 1, KUN_BUF_TEMP = 2 } KunGpuBufferKind;
@@ -52,6 +52,11 @@ typedef struct {
     int32_t nseg;
     int64_t n_active;          /* seg_off[nseg] */
     int32_t max_seg_len;       /* longest segment (cross-sectional stages) */
+    /* stream mode, optional: device int32[3] = {nseg, n_active, max_seg_len}.
+     * When set, the kernels take the counts from here and the three host
+     * fields above are upper bounds that size the grids, so one captured
+     * graph serves any batch of segments within those bounds. */
+    const int32_t *seg_count;
 } KunGpuStageArgs;
 
 typedef int (*KunGpuLaunchFn)(const KunGpuStageArgs *args, void *cuda_stream);

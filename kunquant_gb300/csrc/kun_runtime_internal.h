@@ -121,4 +121,26 @@ struct StreamStore {
     KunStatus reset(long long stock0, long long count, cudaStream_t st);
 };
 
+// Stage order of a stream module (false on a cycle).
+bool stream_order(const KunGpuModuleDesc *m, std::vector<int> &order);
+
+// Concurrent stages of one tick: stage -> stream, with completion events.
+struct TickSchedule {
+    std::vector<int> stream_of;
+    std::vector<std::vector<int>> preds;
+    std::vector<cudaStream_t> streams;  // [0] is the caller's stream (unused slot)
+    std::vector<cudaEvent_t> done;      // per stage
+    std::vector<cudaEvent_t> join;      // per stream
+    cudaEvent_t fork = nullptr;
+};
+bool make_tick_schedule(const KunGpuModuleDesc *m, const std::vector<int> &order, int nstreams, TickSchedule &s);
+void free_tick_schedule(TickSchedule &s);
+
+// Enqueue one tick of every stage of `store` for the segments described by
+// the device arrays; with `d_seg_count` the host counts are upper bounds.
+KunStatus enqueue_tick(const StreamStore &store, const std::vector<int> &order, const int32_t *d_seg_off,
+                       const int32_t *d_seg_stock0, const int64_t *d_tick, int nseg, long long n_active,
+                       int max_len, cudaStream_t st, const int32_t *d_seg_count = nullptr,
+                       const TickSchedule *sched = nullptr);
+
 }  // namespace kungpu

@@ -9,6 +9,7 @@
 // device-side tick counter, so ticks can be queued without host round trips.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
@@ -118,13 +119,71 @@ KunStatus StreamStore::reset(long long stock0, long long count, cudaStream_t st)
     return KUN_SUCCESS;
 }
 
-// Enqueue one tick of every stage for the segments in d_seg / d_tick.
+bool make_tick_schedule(const KunGpuModuleDesc *m, const std::vector<int> &order, int nstreams, TickSchedule &s) {
+    int ns = m->num_stages;
+    nstreams = std::max(1, nstreams);
+    s.preds.assign(ns, {});
+    for (int i = 0; i < ns; i++)
+        for (int d = 0; d < m->stages[i].num_deps; d++)
+            if (m->stages[i].deps[d] >= 0) s.preds[m->stages[i].deps[d]].push_back(i);
+    // continue a predecessor's chain when it is that stream's tail, else the
+    // stream with the least work
+    s.stream_of.assign(ns, 0);
+    std::vector<int> tail(nstreams, -1), load(nstreams, 0);
+    for (int si : order) {
+        int pick = -1;
+        for (int d : s.preds[si])
+            for (int k = 0; k < nstreams; k++)
+                if (tail[k] == d) pick = k;
+        if (pick < 0) pick = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        s.stream_of[si] = pick;
+        tail[pick] = si;
+        load[pick] += m->stages[si].num_kernels > 0 ? m->stages[si].num_kernels : 1;
+    }
+    s.streams.assign(nstreams, nullptr);
+    for (int k = 1; k < nstreams; k++)
+        if (cudaStreamCreateWithFlags(&s.streams[k], cudaStreamNonBlocking) != cudaSuccess) return false;
+    s.done.assign(ns, nullptr);
+    for (int i = 0; i < ns; i++)
+        if (cudaEventCreateWithFlags(&s.done[i], cudaEventDisableTiming) != cudaSuccess) return false;
+    s.join.assign(nstreams, nullptr);
+    for (int k = 0; k < nstreams; k++)
+        if (cudaEventCreateWithFlags(&s.join[k], cudaEventDisableTiming) != cudaSuccess) return false;
+    return cudaEventCreateWithFlags(&s.fork, cudaEventDisableTiming) == cudaSuccess;
+}
+
+void free_tick_schedule(TickSchedule &s) {
+    for (size_t k = 1; k < s.streams.size(); k++)
+        if (s.streams[k]) cudaStreamDestroy(s.streams[k]);
+    for (auto e : s.done)
+        if (e) cudaEventDestroy(e);
+    for (auto e : s.join)
+        if (e) cudaEventDestroy(e);
+    if (s.fork) cudaEventDestroy(s.fork);
+    s = TickSchedule();
+}
+
+// Enqueue one tick of every stage for the segments in d_seg / d_tick: in
+// order on `st`, or with `sched`, on its streams (forked from and joined back
+// into `st`) with events for the cross-stream dependencies.
 KunStatus enqueue_tick(const StreamStore &store, const std::vector<int> &order, const int32_t *d_seg_off,
                        const int32_t *d_seg_stock0, const int64_t *d_tick, int nseg, long long n_active,
-                       int max_len, cudaStream_t st) {
+                       int max_len, cudaStream_t st, const int32_t *d_seg_count, const TickSchedule *sched) {
     const KunGpuModuleDesc *m = store.m;
+    const bool multi = sched && sched->streams.size() > 1;
+    if (multi) {
+        cudaEventRecord(sched->fork, st);
+        for (size_t k = 1; k < sched->streams.size(); k++) cudaStreamWaitEvent(sched->streams[k], sched->fork, 0);
+    }
     for (int si : order) {
         const KunGpuStageDesc &d = m->stages[si];
+        cudaStream_t sst = st;
+        if (multi) {
+            int k = sched->stream_of[si];
+            sst = k == 0 ? st : sched->streams[k];
+            for (int pd : sched->preds[si])
+                if (sched->stream_of[pd] != k) cudaStreamWaitEvent(sst, sched->done[pd], 0);
+        }
         KunGpuStageArgs a;
         memset(&a, 0, sizeof a);
         a.buffers = store.rings.data();
@@ -139,12 +198,19 @@ KunStatus enqueue_tick(const StreamStore &store, const std::vector<int> &order, 
         a.nseg = nseg;
         a.n_active = n_active;
         a.max_seg_len = max_len;
-        int rc = d.launch(&a, (void *)st);
+        a.seg_count = d_seg_count;
+        int rc = d.launch(&a, (void *)sst);
         if (rc) {
             set_error("stage %d (%s) failed: %s", si, d.name, cudaGetErrorString((cudaError_t)rc));
             return KUN_CUDA_ERROR;
         }
+        if (multi) cudaEventRecord(sched->done[si], sst);
     }
+    if (multi)
+        for (size_t k = 1; k < sched->streams.size(); k++) {
+            cudaEventRecord(sched->join[k], sched->streams[k]);
+            cudaStreamWaitEvent(st, sched->join[k], 0);
+        }
     return KUN_SUCCESS;
 }
 

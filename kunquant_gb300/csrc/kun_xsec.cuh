@@ -1,8 +1,9 @@
 // Cross-sectional kernels: one thread block per time step (row of the [T][S]
 // layout).
-//  - Rank (cpp/Kun/Rank.hpp:13-57): the row's non-NaN values are sorted in
-//    shared memory (bitonic network over order-preserving integer keys; NaNs
-//    sort last), then every stock binary-searches its equal range;
+//  - Rank (cpp/Kun/Rank.hpp:13-57): the row's non-NaN values are sorted by a
+//    register/shuffle/shared-memory bitonic network over order-preserving
+//    integer keys (NaNs sort last), then every stock binary-searches its
+//    equal range;
 //    out = T(sum) / T(cnt) / T(n) with the integer rank sum of the range.
 //  - Scale (cpp/Kun/Scale.hpp:14-46): the sum of |x| over non-NaN stocks in
 //    stock order (sequential, as the reference adds), then x / sum.
@@ -42,22 +43,37 @@ template <> struct SortKey<double> {
 
 constexpr int kRankThreads = 1024;
 
-// Rank of one row by the whole block: keys[P] and cnt_warp are shared memory.
-template <typename T>
+// Rank of one row by the whole block.  The row's keys (NaN -> max key) are
+// sorted with a bitonic network over P = a power of two >= the row length:
+// thread t holds positions [t*ITEMS, (t+1)*ITEMS) in registers, so the
+// network's exchanges at distance j < ITEMS stay in registers, j < 32*ITEMS
+// go through warp shuffles, and only the longer ones pass through shared
+// memory (keys[e*nt + t], conflict-free) with a block barrier.  Each stock
+// then binary-searches the equal range of its value in the sorted keys.
+template <typename K>
+__device__ __forceinline__ void bitonic_keep(K &mine, K other, bool lower, bool up) {
+    K mn = other < mine ? other : mine, mx = other < mine ? mine : other;
+    mine = (lower == up) ? mn : mx;
+}
+
+template <typename T, int ITEMS>
 __device__ __forceinline__ void rank_one_row(const T *__restrict__ row, T *__restrict__ orow, long long S, int P,
                                              typename SortKey<T>::K *keys, int *cnt_warp) {
     using SK = SortKey<T>;
     using K = typename SK::K;
     const int tid = threadIdx.x;
+    const int nt = P / ITEMS;  // threads holding keys (P >= ITEMS)
+    K r[ITEMS];
     int local = 0;
-    for (int i = tid; i < P; i += blockDim.x) {
-        K k = SK::kMax;
-        if (i < S) {
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++) {
+        r[e] = SK::kMax;
+        const long long i = (long long)tid * ITEMS + e;
+        if (tid < nt && i < S) {
             T x = row[i];
-            k = SK::enc(x);
+            r[e] = SK::enc(x);
             local += (x == x);
         }
-        keys[i] = k;
     }
     for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
     if ((tid & 31) == 0) cnt_warp[tid >> 5] = local;
@@ -65,61 +81,113 @@ __device__ __forceinline__ void rank_one_row(const T *__restrict__ row, T *__res
     int n = 0;
     for (int w = 0; w < (int)(blockDim.x >> 5); w++) n += cnt_warp[w];
     for (int k = 2; k <= P; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = tid; i < P; i += blockDim.x) {
-                int ixj = i ^ j;
-                if (ixj > i) {
-                    K a = keys[i], b = keys[ixj];
-                    bool up = (i & k) == 0;
-                    if ((a > b) == up) { keys[i] = b; keys[ixj] = a; }
+        for (int j = k >> 1; j >= ITEMS; j >>= 1) {
+            if (j >= ITEMS * 32) {
+                const int m = j / ITEMS;
+                if (tid < nt) {
+#pragma unroll
+                    for (int e = 0; e < ITEMS; e++) keys[e * nt + tid] = r[e];
+                }
+                __syncthreads();
+                if (tid < nt) {
+                    const int pt = tid ^ m;
+                    const bool lower = (tid & m) == 0;
+#pragma unroll
+                    for (int e = 0; e < ITEMS; e++) {
+                        const int i = tid * ITEMS + e;
+                        bitonic_keep(r[e], keys[e * nt + pt], lower, (i & k) == 0);
+                    }
+                }
+                __syncthreads();
+            } else {
+                const int m = j / ITEMS;
+                const bool lower = (tid & m) == 0;
+#pragma unroll
+                for (int e = 0; e < ITEMS; e++) {
+                    const int i = tid * ITEMS + e;
+                    K o = __shfl_xor_sync(0xffffffffu, r[e], m);
+                    bitonic_keep(r[e], o, lower, (i & k) == 0);
                 }
             }
-            __syncthreads();
+        }
+        // distances below ITEMS: within the thread, unrolled so that r stays
+        // in registers
+#pragma unroll
+        for (int j = ITEMS / 2; j > 0; j >>= 1) {
+            if (j < k) {
+#pragma unroll
+                for (int e = 0; e < ITEMS; e++) {
+                    if ((e & j) == 0) {
+                        const int i = tid * ITEMS + e;
+                        const bool up = (i & k) == 0;
+                        K a = r[e], b = r[e ^ j];
+                        if ((a > b) == up) {
+                            r[e] = b;
+                            r[e ^ j] = a;
+                        }
+                    }
+                }
+            }
         }
     }
-    for (int i = tid; i < S; i += blockDim.x) {
+    // sorted position p = t*ITEMS + e lives at keys[e*nt + t]
+    if (tid < nt) {
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) keys[e * nt + tid] = r[e];
+    }
+    __syncthreads();
+    auto at = [&](int p) { return SK::dec(keys[(p % ITEMS) * nt + p / ITEMS]); };
+    for (long long i = tid; i < S; i += blockDim.x) {
         T x = row[i];
-        T r;
+        T res;
         if (x != x) {
-            r = knan<T>();
+            res = knan<T>();
         } else {
             int lo = 0, hi = n;
-            while (lo < hi) { int m = (lo + hi) >> 1; if (SK::dec(keys[m]) < x) lo = m + 1; else hi = m; }
+            while (lo < hi) { int m = (lo + hi) >> 1; if (at(m) < x) lo = m + 1; else hi = m; }
             long long start = lo;
             hi = n;
-            while (lo < hi) { int m = (lo + hi) >> 1; if (x < SK::dec(keys[m])) hi = m; else lo = m + 1; }
+            while (lo < hi) { int m = (lo + hi) >> 1; if (x < at(m)) hi = m; else lo = m + 1; }
             long long end = lo;
             long long sum = (start + end + 1) * (end - start) / 2;
-            r = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
+            res = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
         }
-        orow[i] = r;
+        orow[i] = res;
     }
     __syncthreads();
 }
 
-template <typename T>
+// keys per thread for a sort of P keys by kRankThreads threads
+inline int rank_items(int P) { return P <= 8 * kRankThreads ? 8 : (P <= 16 * kRankThreads ? 16 : 32); }
+
+template <typename T, int ITEMS>
 __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ in, T *__restrict__ out,
                                                           long long S, long long length, int P) {
     using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
     for (long long t = blockIdx.x; t < length; t += gridDim.x)
-        rank_one_row<T>(in + t * S, out + t * S, S, P, reinterpret_cast<K *>(smem_raw), cnt_warp);
+        rank_one_row<T, ITEMS>(in + t * S, out + t * S, S, P, reinterpret_cast<K *>(smem_raw), cnt_warp);
 }
 
 // stream mode: one block per segment, each at its own ring row
-template <typename T>
+template <typename T, int ITEMS>
 __global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restrict__ in, int w_in, T *__restrict__ out,
                                                               int w_out, long long cap, const int32_t *seg_off,
                                                               const int32_t *seg_stock0, const long long *seg_tick,
-                                                              int P) {
+                                                              int P, const int32_t *cnt) {
     using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
     const int k = blockIdx.x;
+    if (cnt && k >= cnt[0]) return;
     const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
-    rank_one_row<T>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, P,
-                    reinterpret_cast<K *>(smem_raw), cnt_warp);
+    // sort only the power of two this segment needs (P bounds every segment)
+    if (len > P) return;
+    int Pk = ITEMS;
+    while (Pk < len) Pk <<= 1;
+    rank_one_row<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, Pk,
+                           reinterpret_cast<K *>(smem_raw), cnt_warp);
 }
 
 template <typename T>
@@ -170,9 +238,11 @@ __global__ void __launch_bounds__(256) diffwsum_rows(const T *__restrict__ in0, 
 template <typename T>
 __global__ void __launch_bounds__(256) scale_segments(const T *__restrict__ in, int w_in, T *__restrict__ out,
                                                       int w_out, long long cap, const int32_t *seg_off,
-                                                      const int32_t *seg_stock0, const long long *seg_tick) {
+                                                      const int32_t *seg_stock0, const long long *seg_tick,
+                                                      const int32_t *cnt) {
     __shared__ T total;
     const int k = blockIdx.x;
+    if (cnt && k >= cnt[0]) return;
     const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
     const T *row = in + (n % w_in) * cap + s0;
     T *orow = out + (n % w_out) * cap + s0;
@@ -196,9 +266,10 @@ template <typename T>
 __global__ void __launch_bounds__(256) diffwsum_segments(const T *__restrict__ in0, int w0, const T *__restrict__ in1,
                                                          int w1, T *__restrict__ out, int w_out, long long cap,
                                                          const int32_t *seg_off, const int32_t *seg_stock0,
-                                                         const long long *seg_tick) {
+                                                         const long long *seg_tick, const int32_t *cnt) {
     __shared__ T total;
     const int k = blockIdx.x;
+    if (cnt && k >= cnt[0]) return;
     const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
     const T *a = in0 + (n % w0) * cap + s0, *b = in1 + (n % w1) * cap + s0;
     T *orow = out + (n % w_out) * cap + s0;
@@ -223,20 +294,31 @@ inline int kun_num_sms() {
     return n;
 }
 
-template <typename T>
-inline int launch_rank(const T *in, T *out, long long S, long long length, cudaStream_t st) {
+template <typename T, int ITEMS>
+inline int launch_rank_items(const T *in, T *out, long long S, long long length, int P, cudaStream_t st) {
     using K = typename SortKey<T>::K;
-    int P = 1;
-    while (P < S) P <<= 1;
     size_t smem = (size_t)P * sizeof(K);
-    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
     if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(rank_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e =
+            cudaFuncSetAttribute(rank_rows<T, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
     long long grid = length < (long long)kun_num_sms() * 2 ? length : (long long)kun_num_sms() * 2;
-    rank_rows<T><<<(unsigned)grid, kRankThreads, smem, st>>>(in, out, S, length, P);
+    rank_rows<T, ITEMS><<<(unsigned)grid, kRankThreads, smem, st>>>(in, out, S, length, P);
     return (int)cudaGetLastError();
+}
+
+template <typename T>
+inline int launch_rank(const T *in, T *out, long long S, long long length, cudaStream_t st) {
+    using K = typename SortKey<T>::K;
+    int P = 8;
+    while (P < S) P <<= 1;
+    if ((size_t)P * sizeof(K) > 200 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
+    switch (rank_items(P)) {
+    case 8: return launch_rank_items<T, 8>(in, out, S, length, P, st);
+    case 16: return launch_rank_items<T, 16>(in, out, S, length, P, st);
+    default: return launch_rank_items<T, 32>(in, out, S, length, P, st);
+    }
 }
 
 template <typename T>
@@ -262,37 +344,44 @@ inline int launch_diffwsum(const T *in0, const T *in1, T *out, long long S, long
 template <typename T>
 inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long long cap, const int32_t *seg_off,
                                 const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
-                                cudaStream_t st) {
+                                const int32_t *cnt, cudaStream_t st) {
     using K = typename SortKey<T>::K;
-    int P = 1;
+    int P = 8;
     while (P < max_len) P <<= 1;
     size_t smem = (size_t)P * sizeof(K);
-    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(rank_segments<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return (int)e;
+    if (smem > 200 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
+    auto go = [&](auto kernel) {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return (int)e;
+        }
+        kernel<<<(unsigned)nseg, kRankThreads, smem, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0, seg_tick,
+                                                           P, cnt);
+        return (int)cudaGetLastError();
+    };
+    switch (rank_items(P)) {
+    case 8: return go(rank_segments<T, 8>);
+    case 16: return go(rank_segments<T, 16>);
+    default: return go(rank_segments<T, 32>);
     }
-    rank_segments<T><<<(unsigned)nseg, kRankThreads, smem, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0,
-                                                                 seg_tick, P);
-    return (int)cudaGetLastError();
 }
 
 template <typename T>
 inline int launch_scale_segments(const T *in, int w_in, T *out, int w_out, long long cap, const int32_t *seg_off,
                                  const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
-                                 cudaStream_t st) {
+                                 const int32_t *cnt, cudaStream_t st) {
     (void)max_len;
-    scale_segments<T><<<(unsigned)nseg, 256, 0, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0, seg_tick);
+    scale_segments<T><<<(unsigned)nseg, 256, 0, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0, seg_tick, cnt);
     return (int)cudaGetLastError();
 }
 
 template <typename T>
 inline int launch_diffwsum_segments(const T *in0, int w0, const T *in1, int w1, T *out, int w_out, long long cap,
                                     const int32_t *seg_off, const int32_t *seg_stock0, const long long *seg_tick,
-                                    int nseg, int max_len, cudaStream_t st) {
+                                    int nseg, int max_len, const int32_t *cnt, cudaStream_t st) {
     (void)max_len;
     diffwsum_segments<T><<<(unsigned)nseg, 256, 0, st>>>(in0, w0, in1, w1, out, w_out, cap, seg_off, seg_stock0,
-                                                         seg_tick);
+                                                         seg_tick, cnt);
     return (int)cudaGetLastError();
 }
 

@@ -175,14 +175,17 @@ struct {pstruct} {{
   const int32_t* seg_off;
   const int32_t* seg_stock0;
   const long long* seg_tick;
+  const int32_t* cnt;
   int nseg;
   long long n_active, S;
 }};
 
 __global__ void __launch_bounds__(KUN_TS_THREADS) {self.kname}(const {pstruct} P) {{
   const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= P.n_active) return;
-  const int k = kun_segment(P.seg_off, P.nseg, i);
+  const int nseg = P.cnt ? P.cnt[0] : P.nseg;
+  const long long n_active = P.cnt ? (long long)P.cnt[1] : P.n_active;
+  if (i >= n_active) return;
+  const int k = kun_segment(P.seg_off, nseg, i);
   const long long s = P.seg_stock0[k] + (i - P.seg_off[k]);
   const long long n = P.seg_tick[k];
   const long long S = P.S;
@@ -223,7 +226,7 @@ __global__ void {self.kname}_initk(const {pstruct} P) {{
 {fill}
   P.st = ({T}*)a->state; P.si = (int32_t*)a->state_i;
   P.seg_off = a->seg_off; P.seg_stock0 = a->seg_stock0; P.seg_tick = (const long long*)a->seg_tick;
-  P.nseg = a->nseg; P.n_active = a->n_active; P.S = a->num_stocks;
+  P.nseg = a->nseg; P.n_active = a->n_active; P.S = a->num_stocks; P.cnt = a->seg_count;
   if (a->n_active <= 0) return 0;"""
         launch = f"""
 extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
@@ -376,7 +379,7 @@ extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
 {fill}
   if (a->n_active <= 0) return 0;
   return kun::{fn}<{T}>({ring_args}, ({T}*)P.p[{out_slot}], {wout}, a->num_stocks, a->seg_off,
-      a->seg_stock0, (const long long*)a->seg_tick, a->nseg, a->max_seg_len, (cudaStream_t)stream);
+      a->seg_stock0, (const long long*)a->seg_tick, a->nseg, a->max_seg_len, a->seg_count, (cudaStream_t)stream);
 }}
 """
         return src, launch
