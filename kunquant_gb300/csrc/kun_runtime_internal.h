@@ -115,6 +115,8 @@ struct StreamStore {
     std::vector<void *> rings;
     std::vector<void *> st_t, st_i;
     void *d_init = nullptr;  // segment table of one reset
+    void **d_rows = nullptr;  // start of every ring row (all buffers)
+    long long n_rows = 0;
     bool alloc(const KunGpuModuleDesc *mod, long long capacity);
     void release();
     size_t bytes_per_stock() const;

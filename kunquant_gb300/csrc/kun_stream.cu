@@ -20,13 +20,15 @@
 
 namespace kungpu {
 
+// NaN-fill columns [col0, col0 + ncols) of every ring row: row f of the
+// flattened rows of all rings starts at rows[f]
 template <typename T>
-__global__ void fill_rect_nan(T *p, long long pitch, long long rows, long long col0, long long ncols) {
-    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= rows * ncols) return;
-    const long long r = i / ncols, c = i % ncols;
-    p[r * pitch + col0 + c] = (T)__int_as_float(0x7fc00000);
+__global__ void fill_rows_nan(T *const *rows, long long col0, long long ncols) {
+    const long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncols) return;
+    rows[blockIdx.y][col0 + c] = (T)__int_as_float(0x7fc00000);
 }
+
 
 __global__ void advance_tick(long long *tick, int nseg) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -52,6 +54,16 @@ bool StreamStore::alloc(const KunGpuModuleDesc *mod, long long capacity) {
         if (d.state_i_vars && cudaMalloc(&st_i[s], (size_t)d.state_i_vars * cap * 4) != cudaSuccess) return false;
     }
     if (cudaMalloc(&d_init, 4 * sizeof(int64_t)) != cudaSuccess) return false;
+    // row table for one-launch resets
+    std::vector<void *> rowp;
+    for (int b = 0; b < m->num_buffers; b++) {
+        long long w = m->buffers[b].window > 0 ? m->buffers[b].window : 1;
+        for (long long r = 0; r < w; r++) rowp.push_back((char *)rings[b] + (size_t)r * cap * elem);
+    }
+    n_rows = (long long)rowp.size();
+    if (n_rows && cudaMalloc((void **)&d_rows, rowp.size() * sizeof(void *)) != cudaSuccess) return false;
+    if (n_rows && cudaMemcpy(d_rows, rowp.data(), rowp.size() * sizeof(void *), cudaMemcpyHostToDevice) != cudaSuccess)
+        return false;
     return true;
 }
 
@@ -63,6 +75,8 @@ void StreamStore::release() {
     for (auto p : st_i)
         if (p) cudaFree(p);
     if (d_init) cudaFree(d_init);
+    if (d_rows) cudaFree(d_rows);
+    d_rows = nullptr;
     rings.clear();
     st_t.clear();
     st_i.clear();
@@ -81,14 +95,13 @@ size_t StreamStore::bytes_per_stock() const {
 // their op states (the ops' constructors, cpp/Kun/Ops.hpp).
 KunStatus StreamStore::reset(long long stock0, long long count, cudaStream_t st) {
     size_t elem = elem_of(m);
-    for (int b = 0; b < m->num_buffers; b++) {
-        long long w = m->buffers[b].window > 0 ? m->buffers[b].window : 1;
-        long long n = w * count;
-        unsigned grid = (unsigned)((n + 255) / 256);
+    // every ring row in one launch (rows go along grid y, at most 65535 per launch)
+    for (long long r0 = 0; r0 < n_rows; r0 += 65535) {
+        dim3 grid((unsigned)((count + 255) / 256), (unsigned)std::min<long long>(65535, n_rows - r0));
         if (elem == 4)
-            fill_rect_nan<float><<<grid, 256, 0, st>>>((float *)rings[b], cap, w, stock0, count);
+            fill_rows_nan<float><<<grid, 256, 0, st>>>((float *const *)d_rows + r0, stock0, count);
         else
-            fill_rect_nan<double><<<grid, 256, 0, st>>>((double *)rings[b], cap, w, stock0, count);
+            fill_rows_nan<double><<<grid, 256, 0, st>>>((double *const *)d_rows + r0, stock0, count);
     }
     int32_t h_seg[3] = {0, (int32_t)count, (int32_t)stock0};
     cudaMemcpyAsync(d_init, h_seg, sizeof h_seg, cudaMemcpyHostToDevice, st);

@@ -42,6 +42,17 @@ template <> struct SortKey<double> {
 };
 
 constexpr int kRankThreads = 1024;
+constexpr int kRadixMinP = 2048;  // rows at least this long (padded) use the radix sort
+__host__ __device__ inline int skew(int p) { return p + (p >> 5); }
+// keys per thread for a sort of P keys by kRankThreads threads
+__host__ __device__ inline int rank_items(int P) {
+    return P <= 8 * kRankThreads ? 8 : (P <= 16 * kRankThreads ? 16 : 32);
+}
+// key slots of a rank block's shared memory for rows padded to P: the radix
+// sort works on all kRankThreads * ITEMS positions
+__host__ __device__ inline int rank_key_slots(int P) {
+    return (P >= kRadixMinP ? skew(kRankThreads * rank_items(P)) : skew(P)) + 1;
+}
 
 // Rank of one row by the whole block.  The row's keys (NaN -> max key) are
 // sorted with a bitonic network over P = a power of two >= the row length:
@@ -54,6 +65,31 @@ template <typename K>
 __device__ __forceinline__ void bitonic_keep(K &mine, K other, bool lower, bool up) {
     K mn = other < mine ? other : mine, mx = other < mine ? mine : other;
     mine = (lower == up) ? mn : mx;
+}
+
+// out[i] from the sorted non-NaN values (at(p), p < n): the average rank of
+// x's equal range over n (cpp/Kun/Rank.hpp:40-53)
+template <typename T, typename At>
+__device__ __forceinline__ void rank_from_sorted(const T *__restrict__ row, T *__restrict__ orow, long long S, int n,
+                                                 At at) {
+    for (long long i = threadIdx.x; i < S; i += blockDim.x) {
+        T x = row[i];
+        T res;
+        if (x != x) {
+            res = knan<T>();
+        } else {
+            int lo = 0, hi = n;
+            while (lo < hi) { int m = (lo + hi) >> 1; if (at(m) < x) lo = m + 1; else hi = m; }
+            long long start = lo;
+            hi = n;
+            while (lo < hi) { int m = (lo + hi) >> 1; if (x < at(m)) hi = m; else lo = m + 1; }
+            long long end = lo;
+            long long sum = (start + end + 1) * (end - start) / 2;
+            res = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
+        }
+        orow[i] = res;
+    }
+    __syncthreads();
 }
 
 template <typename T, int ITEMS>
@@ -136,29 +172,103 @@ __device__ __forceinline__ void rank_one_row(const T *__restrict__ row, T *__res
         for (int e = 0; e < ITEMS; e++) keys[e * nt + tid] = r[e];
     }
     __syncthreads();
-    auto at = [&](int p) { return SK::dec(keys[(p % ITEMS) * nt + p / ITEMS]); };
-    for (long long i = tid; i < S; i += blockDim.x) {
-        T x = row[i];
-        T res;
-        if (x != x) {
-            res = knan<T>();
-        } else {
-            int lo = 0, hi = n;
-            while (lo < hi) { int m = (lo + hi) >> 1; if (at(m) < x) lo = m + 1; else hi = m; }
-            long long start = lo;
-            hi = n;
-            while (lo < hi) { int m = (lo + hi) >> 1; if (x < at(m)) hi = m; else lo = m + 1; }
-            long long end = lo;
-            long long sum = (start + end + 1) * (end - start) / 2;
-            res = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
-        }
-        orow[i] = res;
-    }
-    __syncthreads();
+    rank_from_sorted<T>(row, orow, S, n, [&](int p) { return SK::dec(keys[(p % ITEMS) * nt + p / ITEMS]); });
 }
 
-// keys per thread for a sort of P keys by kRankThreads threads
-inline int rank_items(int P) { return P <= 8 * kRankThreads ? 8 : (P <= 16 * kRankThreads ? 16 : 32); }
+// Rank of one row by LSD radix sort (4-bit digits, stable), for long rows
+// where the bitonic network's P log^2 P exchanges cost more than the digit
+// passes.  blockDim.x must be kRankThreads; thread t holds positions
+// [t*ITEMS, (t+1)*ITEMS).  Shared memory: the keys (skewed by one slot every
+// 32 against bank conflicts) then 16 x kRankThreads 16-bit digit counters.
+template <typename T, int ITEMS>
+__device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T *__restrict__ orow, long long S,
+                                                   typename SortKey<T>::K *keys, uint16_t *counters,
+                                                   int *cnt_warp) {
+    using SK = SortKey<T>;
+    using K = typename SK::K;
+    constexpr int NT = kRankThreads;
+    const int tid = threadIdx.x;
+    K r[ITEMS];
+    int local = 0;
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++) {
+        r[e] = SK::kMax;
+        const long long i = (long long)tid * ITEMS + e;
+        if (i < S) {
+            T x = row[i];
+            r[e] = SK::enc(x);
+            local += (x == x);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
+    if ((tid & 31) == 0) cnt_warp[tid >> 5] = local;
+    __syncthreads();
+    int n = 0;
+    for (int w = 0; w < NT / 32; w++) n += cnt_warp[w];
+    __syncthreads();
+    __shared__ int warp_tot[NT / 32];
+    for (int shift = 0; shift < (int)(sizeof(K) * 8); shift += 4) {
+#pragma unroll
+        for (int d = 0; d < 16; d++) counters[d * NT + tid] = 0;
+        uint16_t mine[ITEMS];
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) {
+            const int d = (int)((r[e] >> shift) & 15);
+            mine[e] = counters[d * NT + tid]++;
+        }
+        __syncthreads();
+        // exclusive scan of the counters in (digit, thread) order: thread t
+        // takes the 16 consecutive entries [16t, 16t + 16)
+        int part[16];
+        int sum = 0;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            part[q] = sum;
+            sum += counters[tid * 16 + q];
+        }
+        int incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((tid & 31) >= o) incl += v;
+        }
+        if ((tid & 31) == 31) warp_tot[tid >> 5] = incl;
+        __syncthreads();
+        if (tid < 32) {
+            int v = warp_tot[tid];
+            int x = v;
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (tid >= o) x += y;
+            }
+            warp_tot[tid] = x - v;  // exclusive
+        }
+        __syncthreads();
+        const int base = warp_tot[tid >> 5] + incl - sum;
+#pragma unroll
+        for (int q = 0; q < 16; q++) counters[tid * 16 + q] = (uint16_t)(base + part[q]);
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) {
+            const int d = (int)((r[e] >> shift) & 15);
+            keys[skew(counters[d * NT + tid] + mine[e])] = r[e];
+        }
+        __syncthreads();
+        if (shift + 4 < (int)(sizeof(K) * 8)) {
+#pragma unroll
+            for (int e = 0; e < ITEMS; e++) r[e] = keys[skew(tid * ITEMS + e)];
+        }
+        __syncthreads();
+    }
+    rank_from_sorted<T>(row, orow, S, n, [&](int p) { return SK::dec(keys[skew(p)]); });
+}
+
+// shared memory of a rank block sorting up to P keys
+template <typename T>
+inline size_t rank_smem_bytes(int P) {
+    using K = typename SortKey<T>::K;
+    size_t keys = ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16;
+    return P >= kRadixMinP ? keys + 16 * (size_t)kRankThreads * sizeof(uint16_t) : keys;
+}
 
 template <typename T, int ITEMS>
 __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ in, T *__restrict__ out,
@@ -166,8 +276,14 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ 
     using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
-    for (long long t = blockIdx.x; t < length; t += gridDim.x)
-        rank_one_row<T, ITEMS>(in + t * S, out + t * S, S, P, reinterpret_cast<K *>(smem_raw), cnt_warp);
+    K *keys = reinterpret_cast<K *>(smem_raw);
+    uint16_t *counters = reinterpret_cast<uint16_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    for (long long t = blockIdx.x; t < length; t += gridDim.x) {
+        if (P >= kRadixMinP)
+            rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, cnt_warp);
+        else
+            rank_one_row<T, ITEMS>(in + t * S, out + t * S, S, P, keys, cnt_warp);
+    }
 }
 
 // stream mode: one block per segment, each at its own ring row
@@ -186,8 +302,13 @@ __global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restric
     if (len > P) return;
     int Pk = ITEMS;
     while (Pk < len) Pk <<= 1;
-    rank_one_row<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, Pk,
-                           reinterpret_cast<K *>(smem_raw), cnt_warp);
+    K *keys = reinterpret_cast<K *>(smem_raw);
+    uint16_t *counters = reinterpret_cast<uint16_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    if (Pk >= kRadixMinP)
+        rank_one_row_radix<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys, counters,
+                                     cnt_warp);
+    else
+        rank_one_row<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, Pk, keys, cnt_warp);
 }
 
 template <typename T>
@@ -239,17 +360,24 @@ template <typename T>
 __global__ void __launch_bounds__(256) scale_segments(const T *__restrict__ in, int w_in, T *__restrict__ out,
                                                       int w_out, long long cap, const int32_t *seg_off,
                                                       const int32_t *seg_stock0, const long long *seg_tick,
-                                                      const int32_t *cnt) {
+                                                      const int32_t *cnt, int max_len) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *row_s = reinterpret_cast<T *>(smem_raw);
     __shared__ T total;
     const int k = blockIdx.x;
     if (cnt && k >= cnt[0]) return;
     const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
+    if (len > max_len) return;
     const T *row = in + (n % w_in) * cap + s0;
     T *orow = out + (n % w_out) * cap + s0;
+    // stage the row in shared memory, then one thread adds in stock order
+    // (the reference's sequential sum)
+    for (long long i = threadIdx.x; i < len; i += blockDim.x) row_s[i] = row[i];
+    __syncthreads();
     if (threadIdx.x == 0) {
         T sum = 0;
         for (long long i = 0; i < len; i++) {
-            T x = row[i];
+            T x = row_s[i];
             if (x == x) sum = kadd(sum, kabs(x));
         }
         total = sum;
@@ -257,7 +385,7 @@ __global__ void __launch_bounds__(256) scale_segments(const T *__restrict__ in, 
     __syncthreads();
     const T sum = total;
     for (long long i = threadIdx.x; i < len; i += blockDim.x) {
-        T x = row[i];
+        T x = row_s[i];
         orow[i] = (x == T(0) && sum == T(0)) ? knan<T>() : kdiv(x, sum);
     }
 }
@@ -296,8 +424,7 @@ inline int kun_num_sms() {
 
 template <typename T, int ITEMS>
 inline int launch_rank_items(const T *in, T *out, long long S, long long length, int P, cudaStream_t st) {
-    using K = typename SortKey<T>::K;
-    size_t smem = (size_t)P * sizeof(K);
+    size_t smem = rank_smem_bytes<T>(P);
     if (smem > 48 * 1024) {
         cudaError_t e =
             cudaFuncSetAttribute(rank_rows<T, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -310,10 +437,9 @@ inline int launch_rank_items(const T *in, T *out, long long S, long long length,
 
 template <typename T>
 inline int launch_rank(const T *in, T *out, long long S, long long length, cudaStream_t st) {
-    using K = typename SortKey<T>::K;
     int P = 8;
     while (P < S) P <<= 1;
-    if ((size_t)P * sizeof(K) > 200 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
+    if (rank_smem_bytes<T>(P) > 200 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
     switch (rank_items(P)) {
     case 8: return launch_rank_items<T, 8>(in, out, S, length, P, st);
     case 16: return launch_rank_items<T, 16>(in, out, S, length, P, st);
@@ -345,10 +471,9 @@ template <typename T>
 inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long long cap, const int32_t *seg_off,
                                 const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
                                 const int32_t *cnt, cudaStream_t st) {
-    using K = typename SortKey<T>::K;
     int P = 8;
     while (P < max_len) P <<= 1;
-    size_t smem = (size_t)P * sizeof(K);
+    size_t smem = rank_smem_bytes<T>(P);
     if (smem > 200 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
     auto go = [&](auto kernel) {
         if (smem > 48 * 1024) {
@@ -370,8 +495,14 @@ template <typename T>
 inline int launch_scale_segments(const T *in, int w_in, T *out, int w_out, long long cap, const int32_t *seg_off,
                                  const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
                                  const int32_t *cnt, cudaStream_t st) {
-    (void)max_len;
-    scale_segments<T><<<(unsigned)nseg, 256, 0, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0, seg_tick, cnt);
+    size_t smem = (size_t)max_len * sizeof(T);
+    if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(scale_segments<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return (int)e;
+    }
+    scale_segments<T><<<(unsigned)nseg, 256, smem, st>>>(in, w_in, out, w_out, cap, seg_off, seg_stock0, seg_tick,
+                                                         cnt, max_len);
     return (int)cudaGetLastError();
 }
 

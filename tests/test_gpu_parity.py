@@ -87,3 +87,33 @@ def test_multistream_graph_replay_bit_exact():
         got = {k: v.cpu().numpy() for k, v in outs.items()}
         bad = compare_exact(got, want)
         assert not bad, f"run {it}: {len(bad)} outputs differ: {dict(list(bad.items())[:5])}"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fixture,S", [("rank_ties_nan", 2047), ("rank_ties_nan", 2048), ("rank_ties_nan", 5000),
+                                       ("rank_ties_nan", 8192), ("rank_ties_nan", 9000),
+                                       ("rank2_exact", 3000), ("rank029_f64", 3000)])
+def test_rank_long_rows_bit_exact(fixture, S):
+    """Rows long enough for the radix-sort rank (and the wider 16-key form
+    above 8192 stocks), with ties, +-0 and NaN rows, against the oracle."""
+    from kunquant_gb300 import build
+    from tests import golden_util as G
+    spec = G.load(fixture)[0]
+    dt = np.float32 if spec["dtype"] == "float" else np.float64
+    rng = np.random.default_rng(S)
+    T = 40 if fixture != "rank029_f64" else 30
+    a = (rng.integers(0, 50, size=(T, S)) / 7).astype(dt)     # many ties
+    a[3, :] = np.nan
+    a[5, ::3] = np.nan
+    a[7, :] = 0.0
+    a[7, ::2] = -0.0
+    a[9] = rng.random(S).astype(dt)                              # no ties
+    key = "units_" + fixture
+    if key not in _libs:
+        _libs[key] = kr.Library.load(build.build_module_library([spec], "kun_rank_" + fixture))
+    mod = _libs[key].getModule(spec["name"])
+    ex = kr.createSingleThreadExecutor()
+    got = kr.runGraph(ex, mod, {"a": a}, 0, T)
+    want = OracleProgram(spec).run({"a": a})
+    bad = compare_exact(got, want)
+    assert not bad, f"{len(bad)} outputs differ: {dict(list(bad.items())[:5])}"
