@@ -178,60 +178,101 @@ __device__ __forceinline__ void rank_one_row(const T *__restrict__ row, T *__res
 // Rank of one row by LSD radix sort (4-bit digits, stable), for long rows
 // where the bitonic network's P log^2 P exchanges cost more than the digit
 // passes.  blockDim.x must be kRankThreads; thread t holds positions
-// [t*ITEMS, (t+1)*ITEMS).  Shared memory: the keys (skewed by one slot every
-// 32 against bank conflicts) then 16 x kRankThreads 16-bit digit counters.
+// [t*ITEMS, (t+1)*ITEMS).  Only the non-NaN values are sorted, each with its
+// stock index, and only the digits in which they differ are passed over.  The
+// ranks then come from the sorted run of equal values around each position
+// (two block scans) instead of binary searches.  Shared memory: keys, 16 x
+// kRankThreads 32-bit digit counters and 16-bit stock indices, each skewed by
+// one slot every 32 so that counting, scan and reloads are conflict-free.
 template <typename T, int ITEMS>
 __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T *__restrict__ orow, long long S,
-                                                   typename SortKey<T>::K *keys, uint16_t *counters,
-                                                   int *cnt_warp) {
+                                                   typename SortKey<T>::K *keys, uint32_t *counters,
+                                                   uint16_t *idx, int *cnt_warp) {
     using SK = SortKey<T>;
     using K = typename SK::K;
     constexpr int NT = kRankThreads;
-    const int tid = threadIdx.x;
+    constexpr int BITS = (int)sizeof(K) * 8;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ int warp_tot[NT / 32], warp_tot2[NT / 32];
+    __shared__ K red_or[NT / 32], red_and[NT / 32];
     K r[ITEMS];
+    uint16_t ix[ITEMS];
+    bool real[ITEMS];
     int local = 0;
+    K o_or = 0, o_and = ~K(0);
 #pragma unroll
     for (int e = 0; e < ITEMS; e++) {
+        const int i = tid * ITEMS + e;
+        real[e] = false;
         r[e] = SK::kMax;
-        const long long i = (long long)tid * ITEMS + e;
+        ix[e] = (uint16_t)i;
         if (i < S) {
             T x = row[i];
-            r[e] = SK::enc(x);
-            local += (x == x);
+            if (x == x) {
+                real[e] = true;
+                r[e] = SK::enc(x);
+                local++;
+                o_or |= r[e];
+                o_and &= r[e];
+            } else {
+                orow[i] = knan<T>();
+            }
         }
     }
-    for (int o = 16; o > 0; o >>= 1) local += __shfl_xor_sync(0xffffffffu, local, o);
-    if ((tid & 31) == 0) cnt_warp[tid >> 5] = local;
+    for (int o = 16; o > 0; o >>= 1) {
+        local += __shfl_xor_sync(0xffffffffu, local, o);
+        o_or |= __shfl_xor_sync(0xffffffffu, o_or, o);
+        o_and &= __shfl_xor_sync(0xffffffffu, o_and, o);
+    }
+    if (lane == 0) {
+        cnt_warp[warp] = local;
+        red_or[warp] = o_or;
+        red_and[warp] = o_and;
+    }
     __syncthreads();
     int n = 0;
-    for (int w = 0; w < NT / 32; w++) n += cnt_warp[w];
-    __syncthreads();
-    __shared__ int warp_tot[NT / 32];
-    for (int shift = 0; shift < (int)(sizeof(K) * 8); shift += 4) {
+    K orv = 0, andv = ~K(0);
+    for (int w = 0; w < NT / 32; w++) {
+        n += cnt_warp[w];
+        orv |= red_or[w];
+        andv &= red_and[w];
+    }
+    if (n == 0) {  // an all-NaN row: its outputs are written above
+        __syncthreads();
+        return;
+    }
+    // digits in which the values differ (at least one pass, which also
+    // compacts the non-NaN values to positions [0, n))
+    K todo = orv ^ andv;
+    if (todo == 0) todo = 1;
+    int last_shift = 0;
+    for (int sh = 0; sh < BITS; sh += 4)
+        if ((todo >> sh) & 15) last_shift = sh;
+    for (int shift = 0; shift < BITS; shift += 4) {
+        if (((todo >> shift) & 15) == 0) continue;
 #pragma unroll
-        for (int d = 0; d < 16; d++) counters[d * NT + tid] = 0;
+        for (int d = 0; d < 16; d++) counters[skew(d * NT + tid)] = 0;
         uint16_t mine[ITEMS];
 #pragma unroll
         for (int e = 0; e < ITEMS; e++) {
-            const int d = (int)((r[e] >> shift) & 15);
-            mine[e] = counters[d * NT + tid]++;
+            mine[e] = 0;
+            if (real[e]) {
+                const int d = (int)((r[e] >> shift) & 15);
+                mine[e] = (uint16_t)(counters[skew(d * NT + tid)]++);
+            }
         }
         __syncthreads();
         // exclusive scan of the counters in (digit, thread) order: thread t
         // takes the 16 consecutive entries [16t, 16t + 16)
-        int part[16];
         int sum = 0;
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-            part[q] = sum;
-            sum += counters[tid * 16 + q];
-        }
+        for (int q = 0; q < 16; q++) sum += counters[skew(tid * 16 + q)];
         int incl = sum;
         for (int o = 1; o < 32; o <<= 1) {
             int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if ((tid & 31) >= o) incl += v;
+            if (lane >= o) incl += v;
         }
-        if ((tid & 31) == 31) warp_tot[tid >> 5] = incl;
+        if (lane == 31) warp_tot[warp] = incl;
         __syncthreads();
         if (tid < 32) {
             int v = warp_tot[tid];
@@ -243,23 +284,108 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
             warp_tot[tid] = x - v;  // exclusive
         }
         __syncthreads();
-        const int base = warp_tot[tid >> 5] + incl - sum;
+        int run = warp_tot[warp] + incl - sum;
 #pragma unroll
-        for (int q = 0; q < 16; q++) counters[tid * 16 + q] = (uint16_t)(base + part[q]);
+        for (int q = 0; q < 16; q++) {
+            const int v = (int)counters[skew(tid * 16 + q)];
+            counters[skew(tid * 16 + q)] = (uint32_t)run;
+            run += v;
+        }
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < ITEMS; e++) {
-            const int d = (int)((r[e] >> shift) & 15);
-            keys[skew(counters[d * NT + tid] + mine[e])] = r[e];
+            if (real[e]) {
+                const int d = (int)((r[e] >> shift) & 15);
+                const int pos = skew((int)counters[skew(d * NT + tid)] + mine[e]);
+                keys[pos] = r[e];
+                idx[pos] = ix[e];
+            }
         }
         __syncthreads();
-        if (shift + 4 < (int)(sizeof(K) * 8)) {
+        if (shift != last_shift) {
 #pragma unroll
-            for (int e = 0; e < ITEMS; e++) r[e] = keys[skew(tid * ITEMS + e)];
+            for (int e = 0; e < ITEMS; e++) {
+                const int p = tid * ITEMS + e;
+                real[e] = p < n;
+                if (real[e]) {
+                    r[e] = keys[skew(p)];
+                    ix[e] = idx[skew(p)];
+                }
+            }
         }
         __syncthreads();
     }
-    rank_from_sorted<T>(row, orow, S, n, [&](int p) { return SK::dec(keys[skew(p)]); });
+    // Equal runs of the sorted values: start(p) = the last run boundary at or
+    // before p (block max-scan), end(p) = one past the run (block min-scan
+    // from the right).  Equality is the values' (-0 == +0), not the keys'.
+    T v[ITEMS];
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++) {
+        const int p = tid * ITEMS + e;
+        v[e] = p < n ? SK::dec(keys[skew(p)]) : T(0);
+    }
+    const int p0 = tid * ITEMS;
+    const T before = (p0 > 0 && p0 - 1 < n) ? SK::dec(keys[skew(p0 - 1)]) : T(0);
+    const T after = (p0 + ITEMS < n) ? SK::dec(keys[skew(p0 + ITEMS)]) : T(0);
+    int st[ITEMS], en[ITEMS];
+    int m = -1;
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++) {
+        const int p = p0 + e;
+        const T prev = e == 0 ? before : v[e - 1];
+        if (p < n && (p == 0 || !(v[e] == prev))) m = p;
+        st[e] = m;
+    }
+    int mn = 1 << 30;
+#pragma unroll
+    for (int e = ITEMS - 1; e >= 0; e--) {
+        const int p = p0 + e;
+        const T next = e == ITEMS - 1 ? after : v[e + 1];
+        if (p < n && (p == n - 1 || !(v[e] == next))) mn = p + 1;
+        en[e] = mn;
+    }
+    // forward exclusive max over threads of m, backward exclusive min of mn
+    int fx = m, bx = mn;
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, fx, o);
+        if (lane >= o) fx = max(fx, y);
+        int z = __shfl_down_sync(0xffffffffu, bx, o);
+        if (lane + o < 32) bx = min(bx, z);
+    }
+    if (lane == 31) warp_tot[warp] = fx;
+    if (lane == 0) warp_tot2[warp] = bx;
+    int fex = __shfl_up_sync(0xffffffffu, fx, 1);
+    int bex = __shfl_down_sync(0xffffffffu, bx, 1);
+    if (lane == 0) fex = -1;
+    if (lane == 31) bex = 1 << 30;
+    __syncthreads();
+    if (tid < 32) {
+        int a = warp_tot[tid], b = warp_tot2[tid];
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, a, o);
+            if (tid >= o) a = max(a, y);
+            int z = __shfl_down_sync(0xffffffffu, b, o);
+            if (tid + o < 32) b = min(b, z);
+        }
+        int ae = __shfl_up_sync(0xffffffffu, a, 1);
+        int be = __shfl_down_sync(0xffffffffu, b, 1);
+        warp_tot[tid] = tid == 0 ? -1 : ae;
+        warp_tot2[tid] = tid == 31 ? (1 << 30) : be;
+    }
+    __syncthreads();
+    const int start_in = max(fex, warp_tot[warp]);
+    const int end_in = min(bex, warp_tot2[warp]);
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++) {
+        const int p = p0 + e;
+        if (p < n) {
+            const long long start = max(st[e], start_in);
+            const long long end = min(en[e], end_in);
+            const long long sum = (start + end + 1) * (end - start) / 2;
+            orow[idx[skew(p)]] = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
+        }
+    }
+    __syncthreads();
 }
 
 // shared memory of a rank block sorting up to P keys
@@ -267,7 +393,9 @@ template <typename T>
 inline size_t rank_smem_bytes(int P) {
     using K = typename SortKey<T>::K;
     size_t keys = ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16;
-    return P >= kRadixMinP ? keys + 16 * (size_t)kRankThreads * sizeof(uint16_t) : keys;
+    return P >= kRadixMinP ? keys + ((size_t)skew(16 * kRankThreads) + 1) * sizeof(uint32_t) +
+                                 (size_t)rank_key_slots(P) * sizeof(uint16_t)
+                           : keys;
 }
 
 template <typename T, int ITEMS>
@@ -277,10 +405,11 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ 
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
     K *keys = reinterpret_cast<K *>(smem_raw);
-    uint16_t *counters = reinterpret_cast<uint16_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + skew(16 * kRankThreads) + 1);
     for (long long t = blockIdx.x; t < length; t += gridDim.x) {
         if (P >= kRadixMinP)
-            rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, cnt_warp);
+            rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, idx, cnt_warp);
         else
             rank_one_row<T, ITEMS>(in + t * S, out + t * S, S, P, keys, cnt_warp);
     }
@@ -303,10 +432,11 @@ __global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restric
     int Pk = ITEMS;
     while (Pk < len) Pk <<= 1;
     K *keys = reinterpret_cast<K *>(smem_raw);
-    uint16_t *counters = reinterpret_cast<uint16_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + skew(16 * kRankThreads) + 1);
     if (Pk >= kRadixMinP)
         rank_one_row_radix<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys, counters,
-                                     cnt_warp);
+                                     idx, cnt_warp);
     else
         rank_one_row<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, Pk, keys, cnt_warp);
 }
@@ -439,7 +569,7 @@ template <typename T>
 inline int launch_rank(const T *in, T *out, long long S, long long length, cudaStream_t st) {
     int P = 8;
     while (P < S) P <<= 1;
-    if (rank_smem_bytes<T>(P) > 200 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
+    if (rank_smem_bytes<T>(P) > 227 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
     switch (rank_items(P)) {
     case 8: return launch_rank_items<T, 8>(in, out, S, length, P, st);
     case 16: return launch_rank_items<T, 16>(in, out, S, length, P, st);
@@ -474,7 +604,7 @@ inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long l
     int P = 8;
     while (P < max_len) P <<= 1;
     size_t smem = rank_smem_bytes<T>(P);
-    if (smem > 200 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
+    if (smem > 227 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
     auto go = [&](auto kernel) {
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
