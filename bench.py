@@ -31,6 +31,11 @@ WORKLOADS = {
                      n_inputs=6, n_outputs=158),
     "alpha101": dict(key="alpha101_f32", module="alpha101", stocks=64, days=260, nan=0.0,
                      n_inputs=6, n_outputs=82),
+    # the same graphs with the fast-stat rolling-moment accumulators
+    "alpha158_fast": dict(key="alpha158_fast_f32", module="alpha158_fast", stocks=5000, days=2500, nan=0.005,
+                          n_inputs=6, n_outputs=158),
+    "alpha101_fast": dict(key="alpha101_fast_f32", module="alpha101_fast", stocks=64, days=260, nan=0.0,
+                          n_inputs=6, n_outputs=82),
 }
 
 

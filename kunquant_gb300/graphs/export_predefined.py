@@ -76,6 +76,14 @@ CONFIGS = {
     "alpha158_f64": (build_alpha158, "alpha158_f64", dict(
         dtype="double", partition_factor=4, input_layout="TS", output_layout="TS",
         options={"opt_reduce": True, "fast_log": True, "no_fast_stat": True})),
+    # fp32 with the reference's fast-stat accumulators (O(1) Kahan-compensated
+    # rolling moments instead of two-pass window loops)
+    "alpha158_fast_f32": (build_alpha158, "alpha158_fast", dict(
+        dtype="float", partition_factor=4, input_layout="TS", output_layout="TS",
+        options={"opt_reduce": True, "fast_log": True, "no_fast_stat": "no_warn"})),
+    "alpha101_fast_f32": (build_alpha101, "alpha101_fast", dict(
+        dtype="float", input_layout="TS", output_layout="TS",
+        options={"opt_reduce": True, "fast_log": True, "no_fast_stat": "no_warn"})),
     "alpha158_stream_f32": (build_alpha158, "alpha158_stream", dict(
         dtype="float", partition_factor=4, input_layout="STREAM", output_layout="STREAM",
         options={"opt_reduce": False, "fast_log": True})),

@@ -229,6 +229,8 @@ def predefined_cases():
         "alpha101_f32": ("alpha101_f32", 16, 200, 0.005, 0),
         "alpha101_f32_start50": ("alpha101_f32", 16, 200, 0.0, 50),
         "alpha158_f64": ("alpha158_f64", 4, 160, 0.005, 0),
+        "alpha158_fast_f32": ("alpha158_fast_f32", 8, 160, 0.005, 0),
+        "alpha101_fast_f32": ("alpha101_fast_f32", 16, 200, 0.005, 0),
         "alpha101_f64": ("alpha101_f64", 8, 200, 0.005, 0),
     }
 
