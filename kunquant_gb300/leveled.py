@@ -23,14 +23,15 @@ from typing import Dict, List, Optional, Set, Tuple
 from . import contraction
 
 SEQ = {"FastWindowedSum", "WindowedLinearRegression", "ExpMovingAvg"}
-UNSUPPORTED = {"Accumulator", "SetAccumulator"}
+UNSUPPORTED: Set[str] = set()
+ACC = {"Accumulator", "SetAccumulator"}
 LR_CONS = {"WindowedLinearRegressionRSqaureImpl", "WindowedLinearRegressionSlopeImpl",
            "WindowedLinearRegressionResiImpl"}
 SL_CONS = {"SkipListQuantile", "SkipListRank", "SkipListMin", "SkipListMax", "SkipListArgMin"}
 REDUCTIONS = {"ReduceAdd", "ReduceMul", "ReduceMin", "ReduceMax", "ReduceArgMax",
               "ReduceArgMin", "ReduceRank", "ReduceDecayLinear"}
-ANCHORS = SEQ | LR_CONS | SL_CONS | REDUCTIONS | {"WindowedTempOutput", "Output", "SkipListState",
-                                                  "ForeachBackWindow"}
+ANCHORS = SEQ | LR_CONS | SL_CONS | REDUCTIONS | ACC | {"WindowedTempOutput", "Output", "SkipListState",
+                                                        "ForeachBackWindow"}
 
 
 def _even_ge(x: int) -> int:
@@ -61,7 +62,66 @@ class StagePlan:
         self.lv: List[int] = [-1] * n
         self.loop_chain: Dict[int, List[int]] = {}
         self._chains()
+        self._acc_groups()
         self._assign()
+
+    # Accumulator recurrences (the fast-stat rolling moments): an
+    # Accumulator's value at row t is what its SetAccumulator stored at row
+    # t-1.  The ops between the reads and the sets of coupled accumulators
+    # form one group that a scan kernel walks through time; every other op
+    # that reads a group value does so from memory at a later level.
+    def _acc_groups(self):
+        ops = self.ops
+        n = len(ops)
+        dep = [False] * n  # depends on some accumulator's value
+        for i, op in enumerate(ops):
+            if op["k"] == "Accumulator" or any(dep[j] for j in op["in"]):
+                dep[i] = True
+                if op.get("p", -1) >= 0:
+                    raise Unsupported("accumulator value used inside a loop")
+        self.state_dep = dep
+        parent = {i: i for i, op in enumerate(ops) if op["k"] == "Accumulator"}
+
+        def find(x):
+            while parent[x] != x:
+                parent[x] = parent[parent[x]]
+                x = parent[x]
+            return x
+
+        on_path: Dict[int, Set[int]] = {}
+        for i, op in enumerate(ops):
+            if op["k"] != "SetAccumulator":
+                continue
+            acc = op["in"][0]
+            # state-dependent ops on the way back from the set to the reads
+            seen, stack = set(), list(op["in"][1:])
+            while stack:
+                j = stack.pop()
+                if j in seen or not dep[j]:
+                    continue
+                seen.add(j)
+                if ops[j]["k"] == "Accumulator":
+                    parent[find(j)] = find(acc)
+                    continue
+                stack.extend(ops[j]["in"])
+            on_path[i] = seen | {i, acc}
+        groups: Dict[int, Set[int]] = {}
+        for i, mem in on_path.items():
+            groups.setdefault(find(ops[i]["in"][0]), set()).update(mem)
+        for a in parent:
+            groups.setdefault(find(a), set()).add(a)
+        for mem in groups.values():
+            for j in mem:
+                ws = self.windowed_source(j)
+                if ops[j]["k"] == "WindowedTempOutput" or (ws is not None and dep[ws]):
+                    # a statistic over a statistic: the inner values would have
+                    # to be written and read back inside the same scan
+                    raise Unsupported("windowed read of a group value inside the group")
+        self.acc_group: Dict[int, int] = {}
+        self.groups: Dict[int, Set[int]] = groups
+        for g, mem in groups.items():
+            for j in mem:
+                self.acc_group[j] = g
 
     # loops merged by merge_loops share reductions: they form one chain
     def _chains(self):
@@ -93,17 +153,62 @@ class StagePlan:
 
     def _assign(self):
         ops, lv = self.ops, self.lv
-        done_chain = set()
+        self._done_chain = set()
         windowed_outputs = set()
         for i, op in enumerate(ops):
             ws = self.windowed_source(i)
             if ws is not None and ops[ws]["k"] == "Output":
                 windowed_outputs.add(ws)
-        for i, op in enumerate(ops):
+        self._windowed_outputs = windowed_outputs
+        # ops that do not depend on accumulator values first; then each
+        # accumulator group goes to the first scan level after its inputs,
+        # then the readers of group values
+        dep = self.state_dep
+        for i in range(len(ops)):
+            if not dep[i]:
+                self._assign_op(i)
+        # a group can read values derived from another group: iterate until
+        # the levels settle (the groups form a DAG)
+        self.group_level: Dict[int, int] = {}
+        for _ in range(len(self.groups) + 2):
+            changed = False
+            for g, mem in self.groups.items():
+                ext = []
+                for j in mem:
+                    if ops[j]["k"] == "Accumulator":
+                        continue
+                    for x in ops[j]["in"]:
+                        if x not in mem:
+                            if dep[x]:
+                                raise Unsupported("accumulator group reads another group's values")
+                            ext.append(self._vl(x))
+                base = max(ext + [-1])
+                L = _odd_ge(base + 1 if base % 2 == 1 else base)
+                if self.group_level.get(g) != L:
+                    self.group_level[g] = L
+                    changed = True
+            for i in range(len(ops)):
+                if dep[i]:
+                    if i in self.acc_group:
+                        lv[i] = self.group_level[self.acc_group[i]]
+                    else:
+                        self._assign_op(i)
+            if not changed:
+                break
+        else:
+            raise Unsupported("accumulator groups do not settle")
+        self._finish_levels()
+
+    def _assign_op(self, i: int):
+        ops, lv = self.ops, self.lv
+        done_chain = self._done_chain
+        windowed_outputs = self._windowed_outputs
+        if True:
+            op = ops[i]
             k = op["k"]
             ins = op["in"]
             if op.get("p", -1) >= 0:
-                continue
+                return
             if k in ("Input", "ConstantOp"):
                 lv[i] = -1
             elif k in ("FastWindowedSum", "WindowedLinearRegression"):
@@ -158,6 +263,9 @@ class StagePlan:
                 lv[i] = _even_ge(lv[ins[0]]) if i in windowed_outputs else None
             else:
                 lv[i] = max([self._vl(j) for j in ins] + [-1])
+
+    def _finish_levels(self):
+        ops, lv = self.ops, self.lv
         # outputs not read back in the stage go to the last parallel level
         top = max([x for x in lv if x is not None] + [0])
         final = _even_ge(top)
@@ -248,6 +356,8 @@ class StagePlan:
             elif k in ("FastWindowedSum", "WindowedLinearRegression"):
                 wreads.add(op["in"][0])
                 deps = [op["in"][0]]
+            elif k == "Accumulator":
+                deps = []  # its input only orders it; the value is the state
             elif k == "SkipListState":
                 wreads.add(self.windowed_source(i))
                 deps = list(op["in"])
@@ -267,6 +377,7 @@ PAR_CHUNK = 32
 REG_WINDOW_MAX = 64
 VEC_U = 4
 SCAN_BLOCK = 16
+WIDE_SERIES = 24
 
 
 class LeveledGen(StageGen):
@@ -311,6 +422,12 @@ class LeveledGen(StageGen):
                         roots = [i] + [j for j, q in enumerate(ops) if q["k"] in LR_CONS and q["in"][0] == i]
                         comp, vr, wr = plan.closure(roots, L)
                         roles.append({"roots": roots, "comp": comp, "vr": vr, "wr": wr})
+                for g, mem in sorted(plan.groups.items()):
+                    if plan.group_level[g] != L:
+                        continue
+                    roots = sorted(j for j in mem if ops[j]["k"] in ACC)
+                    comp, vr, wr = plan.closure(roots, L)
+                    roles.append({"roots": roots, "comp": comp, "vr": vr, "wr": wr})
                 if roles:
                     ks.append({"level": L, "kind": "scan", "roles": roles})
         return ks
@@ -438,6 +555,12 @@ class LeveledGen(StageGen):
             self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.resi({self.val(a[1])});")
         elif k == "ExpMovingAvg":
             self.lines.append(f"{ind}const {T} v{i} = ema{i}.step({self.val(a[0])});")
+        elif k == "Accumulator":
+            self.lines.append(f"{ind}const {T} v{i} = acc{i};")
+        elif k == "SetAccumulator":
+            acc = a[0]
+            self.lines.append(f"{ind}acc{acc} = kun::ksel({self.val(a[1])}) ? {self.val(a[2])} : v{acc};")
+            self.lines.append(f"{ind}const {T} v{i} = acc{acc};")
         elif k == "SkipListState":
             self.lines.append(f"{ind}sl{i}.step({self.val(a[0])}, {self.val(a[1])}, (int)t);")
         elif k in SL_CONS and self._reg_window(a[0]):
@@ -489,6 +612,8 @@ class LeveledGen(StageGen):
         k = op["k"]
         if k == "FastWindowedSum":
             return f"kun::FWSum<{T}> fw{i}({op['window']});"
+        if k == "Accumulator":
+            return f"{T} acc{i} = 0;"
         if k == "WindowedLinearRegression":
             return f"kun::LinReg<{T}, {op['window']}> lr{i};"
         if k == "ExpMovingAvg":
@@ -550,6 +675,14 @@ class LeveledGen(StageGen):
         if self.pf_window is not None and key in self.pf_window:
             return f"{self.pf_window[key]}[u]"
         return super().window_read(src, off)
+
+    def _scan_block(self, role: dict) -> int:
+        """Rows per prefetch block: fewer when the role reads many series, so
+        the prefetched rows stay in registers."""
+        ops = self.ops
+        n = len(role["vr"]) + sum(1 for i in role["comp"]
+                                  if ops[i]["k"] in ("FastWindowedSum", "WindowedLinearRegression", "BackRef"))
+        return SCAN_BLOCK if n <= 6 else (8 if n <= 12 else 4)
 
     def _scan_prefetch(self, role: dict, B: int, ind: str):
         """Scan role body: rows are processed in blocks of B; every series the
@@ -786,7 +919,10 @@ class LeveledGen(StageGen):
                         self.lines.append(f"    sl{i}.step((t - {W} >= tw) ? {self.read_at(src, f't - {W}')} : kun::knan<{T}>(), "
                                           f"{self.read_at(src, 't')}, (int)t);")
                     self.lines.append("  }")
-                if sls or VEC_U <= 1:
+                # wide kernels (many series in and out) keep one row per
+                # iteration: the 4-row form would not fit in registers
+                wide = len(vr) + len(stores) + sum(1 for i in comp if ops[i]["k"] == "Output") > WIDE_SERIES
+                if sls or VEC_U <= 1 or wide:
                     self.lines.append("  for (long long t = t0; t < t1; ++t) {")
                     self._body(comp, vr, stores, loops, "    ")
                 else:
@@ -796,22 +932,24 @@ class LeveledGen(StageGen):
                 grid_y = f"(unsigned)((a->length + {chunk} - 1) / {chunk})"
             else:
                 roles = kd["roles"]
-                allr = set()
-                for r in roles:
-                    allr |= r["vr"] | r["wr"] | {i for i in r["roots"] if i in self.scratch}
-                    for i in r["comp"]:
-                        if ops[i]["k"] == "ExpMovingAvg" and len(ops[i]["in"]) == 2:
-                            allr.add(ops[i]["in"][1])
-                for j in sorted(allr):
-                    self._mem_ptr(j, decl, seen)
                 self.lines.append("  switch (blockIdx.y) {")
                 for ri, r in enumerate(roles):
                     self.lines.append(f"  case {ri}: {{")
+                    # each role declares only the series it touches, so the
+                    # roles do not share live pointer registers
+                    rr = r["vr"] | r["wr"] | {i for i in r["roots"] if i in self.scratch}
+                    for i in r["comp"]:
+                        if ops[i]["k"] == "ExpMovingAvg" and len(ops[i]["in"]) == 2:
+                            rr.add(ops[i]["in"][1])
+                    rdecl: List[str] = []
+                    for j in sorted(rr):
+                        self._mem_ptr(j, rdecl, set())
+                    self.lines += ["  " + x for x in rdecl]
                     for i in sorted(r["comp"]):
                         sd = self._state_decl(i)
                         if sd:
                             self.lines.append(f"    {sd}")
-                    self._scan_prefetch(r, SCAN_BLOCK, "    ")
+                    self._scan_prefetch(r, self._scan_block(r), "    ")
                     self.lines.append("  } break;")
                 self.lines.append("  default: break;")
                 self.lines.append("  }")

@@ -22,6 +22,9 @@ CASES = [
     ("alpha101_f32", "alpha101", 64, 260, 0.0, 50),
     ("alpha158_f64", "alpha158_f64", 32, 260, 0.005, 0),
     ("alpha101_f64", "alpha101_f64", 32, 260, 0.005, 0),
+    ("alpha158_fast_f32", "alpha158_fast", 64, 300, 0.005, 0),
+    ("alpha158_fast_f32", "alpha158_fast", 61, 260, 0.0, 40),
+    ("alpha101_fast_f32", "alpha101_fast", 64, 260, 0.005, 0),
 ]
 
 _programs = {}
