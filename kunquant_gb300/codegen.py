@@ -89,6 +89,9 @@ class StageGen:
         self.tag = tag
         self.dtype = spec["dtype"]
         self.T = "float" if self.dtype == "float" else "double"
+        # type of the running sums (Kahan window sums, window reductions,
+        # regression sums): fp64 in the fp32 "acc64" precision form
+        self.AT = "double" if spec.get("accum") == "f64" else self.T
         self.kname = f"kst_{tag}_{si}"
         self.bufs = spec["buffers"]
         self.slots: Dict[int, int] = {}      # module buffer id -> param slot
@@ -128,8 +131,13 @@ class StageGen:
 
     def val(self, i: int) -> str:
         if self.ops[i]["k"] in REDUCTIONS:
-            return f"r{i}.value()"
+            return self.reduction_value(i, f"r{i}")
         return f"v{i}"
+
+    def reduction_value(self, i: int, obj: str) -> str:
+        if self.ops[i]["k"] == "ReduceAdd" and self.AT != self.T:
+            return f"(({self.T}){obj}.value())"
+        return f"{obj}.value()"
 
     def lit(self, text: str) -> str:
         return literal(text, self.dtype)
@@ -196,7 +204,7 @@ class StageGen:
         k = op["k"]
         T = self.T
         if k == "ReduceAdd":
-            return f"kun::RAdd<{T}> r{r};"
+            return f"kun::RAdd<{self.AT}> r{r};"
         if k == "ReduceMul":
             return f"kun::RMul<{T}> r{r};"
         if k == "ReduceMin":
@@ -288,9 +296,9 @@ class StageGen:
                 decl.append(f"  {T}* __restrict__ b{i} = ({T}*)P.w[{sc}] + s;")
                 decl.append(f"  const long long st{i} = S;")
             elif k == "FastWindowedSum":
-                state.append(f"  kun::FWSum<{T}> fw{i}({op['window']});")
+                state.append(f"  kun::FWSum<{self.AT}> fw{i}({op['window']});")
             elif k == "WindowedLinearRegression":
-                state.append(f"  kun::LinReg<{T}, {op['window']}> lr{i};")
+                state.append(f"  kun::LinReg<{self.AT}, {op['window']}> lr{i};")
             elif k == "ExpMovingAvg":
                 init = f"kun::knan<{T}>()"
                 if len(op["in"]) == 2:
@@ -344,16 +352,16 @@ class StageGen:
             elif k == "BackRef":
                 self.lines.append(f"{ind}const {T} v{i} = {self.window_read(a[0], op['window'])};")
             elif k == "FastWindowedSum":
-                self.lines.append(f"{ind}const {T} v{i} = fw{i}.step({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
+                self.lines.append(f"{ind}const {T} v{i} = ({T})fw{i}.step({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
             elif k == "WindowedLinearRegression":
                 shared = "true" if contraction.regression_shares_square(ops, i) else "false"
                 self.lines.append(f"{ind}lr{i}.template step<{shared}>({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
             elif k == "WindowedLinearRegressionRSqaureImpl":
-                self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.rsq();")
+                self.lines.append(f"{ind}const {T} v{i} = ({T})lr{a[0]}.rsq();")
             elif k == "WindowedLinearRegressionSlopeImpl":
-                self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.slope();")
+                self.lines.append(f"{ind}const {T} v{i} = ({T})lr{a[0]}.slope();")
             elif k == "WindowedLinearRegressionResiImpl":
-                self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.resi({self.val(a[1])});")
+                self.lines.append(f"{ind}const {T} v{i} = ({T})lr{a[0]}.resi({self.val(a[1])});")
             elif k == "ExpMovingAvg":
                 self.lines.append(f"{ind}const {T} v{i} = ema{i}.step({self.val(a[0])});")
             elif k == "SkipListState":

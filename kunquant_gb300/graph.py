@@ -244,7 +244,16 @@ def load_spec(path: str) -> dict:
 
 
 def predefined_spec(name: str) -> dict:
-    """Load a spec shipped in ``kunquant_gb300/graphs`` (``alpha158_f32`` ...)."""
+    """Load a spec shipped in ``kunquant_gb300/graphs`` (``alpha158_f32`` ...).
+
+    ``<base>_acc64_f32`` is the fp32 module ``<base>_f32`` with its running
+    sums (Kahan window sums, two-pass window reductions, regression sums)
+    accumulated in fp64; every other op stays fp32."""
+    if name.endswith("_acc64_f32"):
+        spec = predefined_spec(name[:-len("_acc64_f32")] + "_f32")
+        spec["name"] = spec["name"] + "_acc64"
+        spec["accum"] = "f64"
+        return spec
     for ext in (".json.gz", ".json"):
         p = os.path.join(GRAPH_DIR, name + ext)
         if os.path.exists(p):

@@ -401,7 +401,7 @@ class LeveledGen(StageGen):
             return f"v{i}[u]" if self.vec else f"v{i}"  # materialised earlier, loaded per row
         if self.vec and top:
             if self.ops[i]["k"] in REDUCTIONS:
-                return f"r{i}[u].value()"
+                return self.reduction_value(i, f"r{i}[u]")
             return f"v{i}[u]"
         return super().val(i)
 
@@ -543,16 +543,16 @@ class LeveledGen(StageGen):
         elif k == "BackRef":
             self.lines.append(f"{ind}const {T} v{i} = {self.window_read(a[0], op['window'])};")
         elif k == "FastWindowedSum":
-            self.lines.append(f"{ind}const {T} v{i} = fw{i}.step({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
+            self.lines.append(f"{ind}const {T} v{i} = ({T})fw{i}.step({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
         elif k == "WindowedLinearRegression":
             shared = "true" if contraction.regression_shares_square(ops, i) else "false"
             self.lines.append(f"{ind}lr{i}.template step<{shared}>({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
         elif k == "WindowedLinearRegressionRSqaureImpl":
-            self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.rsq();")
+            self.lines.append(f"{ind}const {T} v{i} = ({T})lr{a[0]}.rsq();")
         elif k == "WindowedLinearRegressionSlopeImpl":
-            self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.slope();")
+            self.lines.append(f"{ind}const {T} v{i} = ({T})lr{a[0]}.slope();")
         elif k == "WindowedLinearRegressionResiImpl":
-            self.lines.append(f"{ind}const {T} v{i} = lr{a[0]}.resi({self.val(a[1])});")
+            self.lines.append(f"{ind}const {T} v{i} = ({T})lr{a[0]}.resi({self.val(a[1])});")
         elif k == "ExpMovingAvg":
             self.lines.append(f"{ind}const {T} v{i} = ema{i}.step({self.val(a[0])});")
         elif k == "Accumulator":
@@ -611,11 +611,11 @@ class LeveledGen(StageGen):
         op, T = self.ops[i], self.T
         k = op["k"]
         if k == "FastWindowedSum":
-            return f"kun::FWSum<{T}> fw{i}({op['window']});"
+            return f"kun::FWSum<{self.AT}> fw{i}({op['window']});"
         if k == "Accumulator":
             return f"{T} acc{i} = 0;"
         if k == "WindowedLinearRegression":
-            return f"kun::LinReg<{T}, {op['window']}> lr{i};"
+            return f"kun::LinReg<{self.AT}, {op['window']}> lr{i};"
         if k == "ExpMovingAvg":
             init = f"kun::knan<{T}>()"
             if len(op["in"]) == 2:
