@@ -90,8 +90,9 @@ class StageGen:
         self.dtype = spec["dtype"]
         self.T = "float" if self.dtype == "float" else "double"
         # type of the running sums (Kahan window sums, window reductions,
-        # regression sums): fp64 in the fp32 "acc64" precision form
-        self.AT = "double" if spec.get("accum") == "f64" else self.T
+        # regression sums): fp64 or two-float compensated fp32 in the
+        # precision forms of an fp32 module
+        self.AT = {"f64": "double", "df32": "kun::DFloat"}.get(spec.get("accum"), self.T)
         self.kname = f"kst_{tag}_{si}"
         self.bufs = spec["buffers"]
         self.slots: Dict[int, int] = {}      # module buffer id -> param slot

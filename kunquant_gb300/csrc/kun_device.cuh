@@ -147,6 +147,74 @@ template <typename T> __device__ __forceinline__ T kexpk(T x) {
     return res;
 }
 
+// ---------------- compensated fp32 ("double-float") running sums
+// A value hi + lo of two floats (|lo| <= ulp(hi)/2) carries about 48 bits.
+// Sums use Knuth's error-free TwoSum on both parts followed by two
+// renormalisations (the accurate double-word addition of Joldes, Muller and
+// Popescu, ACM TOMS 2017); products use the FMA-exact product error; all steps
+// are single fp32 operations, so the accumulators run at fp32 rates.  Used as
+// the accumulator type of the window sums, window reductions and regression
+// sums in the compensated precision form.
+struct DFloat {
+    float hi, lo;
+    __device__ __forceinline__ DFloat() : hi(0.f), lo(0.f) {}
+    __device__ __forceinline__ DFloat(float h) : hi(h), lo(0.f) {}
+    __device__ __forceinline__ DFloat(int i) : hi((float)i), lo(0.f) {}
+    __device__ __forceinline__ DFloat(double d) : hi((float)d), lo((float)(d - (double)(float)d)) {}
+    __device__ __forceinline__ DFloat(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ explicit operator float() const { return __fadd_rn(hi, lo); }
+};
+__device__ __forceinline__ DFloat df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return DFloat(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ DFloat df_fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return DFloat(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ bool kisnan(DFloat x) { return x.hi != x.hi; }
+__device__ __forceinline__ DFloat operator-(DFloat x) { return DFloat(-x.hi, -x.lo); }
+__device__ __forceinline__ DFloat kadd(DFloat x, DFloat y) {
+    const DFloat s = df_two_sum(x.hi, y.hi);
+    if (!isfinite(s.hi)) return DFloat(s.hi, 0.f);
+    const DFloat t = df_two_sum(x.lo, y.lo);
+    const DFloat u = df_fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    return df_fast_two_sum(u.hi, __fadd_rn(u.lo, t.lo));
+}
+__device__ __forceinline__ DFloat ksub(DFloat x, DFloat y) { return kadd(x, -y); }
+__device__ __forceinline__ DFloat kmul(DFloat x, DFloat y) {
+    const float p = __fmul_rn(x.hi, y.hi);
+    if (!isfinite(p)) return DFloat(p, 0.f);
+    float e = __fmaf_rn(x.hi, y.hi, -p);
+    e = __fmaf_rn(x.hi, y.lo, e);
+    e = __fmaf_rn(x.lo, y.hi, e);
+    return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ DFloat kdiv(DFloat x, DFloat y) {
+    const float q1 = __fdiv_rn(x.hi, y.hi);
+    if (!isfinite(q1)) return DFloat(q1, 0.f);
+    const DFloat r = ksub(x, kmul(DFloat(q1), y));
+    const float q2 = __fdiv_rn(r.hi, y.hi);
+    const DFloat q = df_fast_two_sum(q1, q2);
+    const DFloat r2 = ksub(x, kmul(q, y));
+    return kadd(q, DFloat(__fdiv_rn(r2.hi, y.hi)));
+}
+__device__ __forceinline__ DFloat kfma(DFloat a, DFloat b, DFloat c) { return kadd(kmul(a, b), c); }
+template <> __device__ __forceinline__ DFloat knan<DFloat>() { return DFloat(knan<float>(), 0.f); }
+// x + y for a float y: one TwoSum and one renormalisation
+__device__ __forceinline__ DFloat df_add_f(DFloat x, float y) {
+    const DFloat s = df_two_sum(x.hi, y);
+    if (!isfinite(s.hi)) return DFloat(s.hi, 0.f);
+    return df_fast_two_sum(s.hi, __fadd_rn(s.lo, x.lo));
+}
+// x + a*b with the product taken exactly (a*b = p + e)
+__device__ __forceinline__ DFloat df_add_prod(DFloat x, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    if (!isfinite(p)) return DFloat(__fadd_rn(x.hi, p), 0.f);
+    return kadd(x, DFloat(p, __fmaf_rn(a, b, -p)));
+}
+
 // ---------------- reductions of a back-window loop, cpp/Kun/Ops.hpp:468-616
 template <typename T> struct RAdd {
     T v = 0, c = 0;
@@ -171,6 +239,14 @@ template <typename T> struct RAdd {
         v = t;
     }
     __device__ __forceinline__ T value() const { return v; }
+};
+// compensated form: the two-float sum needs no Kahan term of its own
+template <> struct RAdd<DFloat> {
+    DFloat v;
+    __device__ __forceinline__ void step(float x) { v = df_add_f(v, x); }
+    __device__ __forceinline__ void step_fma(float a, float b) { v = df_add_prod(v, a, b); }
+    __device__ __forceinline__ void step_fma_first(float a, float b) { v = df_add_prod(v, a, b); }
+    __device__ __forceinline__ DFloat value() const { return v; }
 };
 template <typename T> struct RMul {
     T v = T(1.0);
@@ -245,6 +321,19 @@ template <typename T> struct FWSum {
         }
         nn = nn - (int)on + (int)cn;
         return nn == 0 ? v : knan<T>();
+    }
+};
+
+template <> struct FWSum<DFloat> {
+    DFloat v;
+    int nn;
+    __device__ __forceinline__ explicit FWSum(int window) : nn(window) {}
+    __device__ __forceinline__ DFloat step(float old, float cur) {
+        const bool on = old != old, cn = cur != cur;
+        if (!on) v = df_add_f(v, -old);
+        if (!cn) v = df_add_f(v, cur);
+        nn = nn - (int)on + (int)cn;
+        return nn == 0 ? v : knan<DFloat>();
     }
 };
 

@@ -248,12 +248,14 @@ def predefined_spec(name: str) -> dict:
 
     ``<base>_acc64_f32`` is the fp32 module ``<base>_f32`` with its running
     sums (Kahan window sums, two-pass window reductions, regression sums)
-    accumulated in fp64; every other op stays fp32."""
-    if name.endswith("_acc64_f32"):
-        spec = predefined_spec(name[:-len("_acc64_f32")] + "_f32")
-        spec["name"] = spec["name"] + "_acc64"
-        spec["accum"] = "f64"
-        return spec
+    accumulated in fp64, and ``<base>_comp_f32`` the same with two-float
+    compensated fp32 sums; every other op stays fp32."""
+    for suffix, accum in (("_acc64_f32", "f64"), ("_comp_f32", "df32")):
+        if name.endswith(suffix):
+            spec = predefined_spec(name[:-len(suffix)] + "_f32")
+            spec["name"] = spec["name"] + suffix[:-4]
+            spec["accum"] = accum
+            return spec
     for ext in (".json.gz", ".json"):
         p = os.path.join(GRAPH_DIR, name + ext)
         if os.path.exists(p):

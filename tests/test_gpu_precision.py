@@ -1,13 +1,14 @@
 """Precision of the fp32 Alpha158 forms against the reference's FP64 TS build.
 
-Three fp32 forms run on the GPU over the same seeded inputs:
+Four fp32 forms run on the GPU over the same seeded inputs:
   * ``alpha158``       -- the reference's default fp32 build: two-pass window
                           moments, Kahan window sums, fp32 regression sums;
   * ``alpha158_fast``  -- the fast-stat build: rolling moments in
                           Kahan-compensated fp32 accumulators;
-  * ``alpha158_acc64`` -- fp32 factor arithmetic with every running sum
+  * ``alpha158_comp``  -- fp32 factor arithmetic with every running sum
                           (Kahan window sums, window reductions, regression
-                          sums) accumulated in fp64 on the GPU.
+                          sums) in two-float compensated fp32;
+  * ``alpha158_acc64`` -- the same running sums in fp64 on the GPU.
 The FP64 oracle (the reference's fp64 TS build restated) is the truth.  For
 each factor the relative error is |got - want| / max(|want|, 1e-3 * m), m the
 factor's median |want| (a floor so that values crossing zero do not divide by
@@ -25,7 +26,7 @@ from kunquant_gb300.graph import predefined_spec
 from oracle.oracle import OracleProgram
 
 FORMS = [("alpha158_f32", "alpha158"), ("alpha158_fast_f32", "alpha158_fast"),
-         ("alpha158_acc64_f32", "alpha158_acc64")]
+         ("alpha158_comp_f32", "alpha158_comp"), ("alpha158_acc64_f32", "alpha158_acc64")]
 
 
 def _errors(got, want):
@@ -84,3 +85,7 @@ def test_alpha158_precision_vs_fp64():
     assert all(acc[f][1] <= 1e-5 for f in names), [f for f in names if acc[f][1] > 1e-5]
     assert sum(acc[f][2] for f in names) == 0
     assert sum(acc[f][0] <= 1e-5 for f in names) > sum(base[f][0] <= 1e-5 for f in names)
+    # the compensated fp32 sums hold the same bound
+    comp = stats["alpha158_comp"]
+    assert all(comp[f][1] <= 1e-5 for f in names), [f for f in names if comp[f][1] > 1e-5]
+    assert sum(comp[f][2] for f in names) == 0
