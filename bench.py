@@ -40,6 +40,9 @@ WORKLOADS = {
     # fp32 factor arithmetic with two-float compensated fp32 running sums
     "alpha158_comp": dict(key="alpha158_comp_f32", module="alpha158_comp", stocks=5000, days=2500, nan=0.005,
                           n_inputs=6, n_outputs=158),
+    # the baseline form: one kernel launch per op, every value through HBM
+    "alpha158_plain": dict(key="alpha158_plain_f32", module="alpha158_plain", stocks=5000, days=2500, nan=0.005,
+                           n_inputs=6, n_outputs=158),
     "alpha101_fast": dict(key="alpha101_fast_f32", module="alpha101_fast", stocks=64, days=260, nan=0.0,
                           n_inputs=6, n_outputs=82),
 }

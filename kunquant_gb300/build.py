@@ -32,7 +32,7 @@ MODULE_FLAGS = COMMON_FLAGS + ["-fmad=false"]
 
 PREDEFINED = ["alpha101_f32", "alpha158_f32", "alpha101_f64", "alpha158_f64", "alpha101_stream_f32",
               "alpha158_stream_f32", "alpha158_fast_f32", "alpha101_fast_f32", "alpha158_acc64_f32",
-              "alpha158_comp_f32"]
+              "alpha158_comp_f32", "alpha158_plain_f32"]
 
 
 def _hash(paths: Iterable[str], extra: str) -> str:

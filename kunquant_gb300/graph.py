@@ -249,12 +249,14 @@ def predefined_spec(name: str) -> dict:
     ``<base>_acc64_f32`` is the fp32 module ``<base>_f32`` with its running
     sums (Kahan window sums, two-pass window reductions, regression sums)
     accumulated in fp64, and ``<base>_comp_f32`` the same with two-float
-    compensated fp32 sums; every other op stays fp32."""
-    for suffix, accum in (("_acc64_f32", "f64"), ("_comp_f32", "df32")):
+    compensated fp32 sums; every other op stays fp32.  ``<base>_plain_f32``
+    is the one-launch-per-op baseline form of ``<base>_f32``."""
+    for suffix, key, val in (("_acc64_f32", "accum", "f64"), ("_comp_f32", "accum", "df32"),
+                             ("_plain_f32", "form", "plain")):
         if name.endswith(suffix):
             spec = predefined_spec(name[:-len(suffix)] + "_f32")
             spec["name"] = spec["name"] + suffix[:-4]
-            spec["accum"] = accum
+            spec[key] = val
             return spec
     for ext in (".json.gz", ".json"):
         p = os.path.join(GRAPH_DIR, name + ext)

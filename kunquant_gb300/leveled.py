@@ -51,8 +51,10 @@ class Unsupported(Exception):
 class StagePlan:
     """Level assignment of one time-series stage."""
 
-    def __init__(self, ops: List[dict]):
+    def __init__(self, ops: List[dict], plain: bool = False):
         self.ops = ops
+        self.plain = plain
+        self.fused_products: Set[int] = set()
         n = len(ops)
         for op in ops:
             if op["k"] in UNSUPPORTED:
@@ -64,6 +66,8 @@ class StagePlan:
         self._chains()
         self._acc_groups()
         self._assign()
+        if plain:
+            self._assign_plain()
 
     # Accumulator recurrences (the fast-stat rolling moments): an
     # Accumulator's value at row t is what its SetAccumulator stored at row
@@ -284,7 +288,81 @@ class StagePlan:
         return self.lv[j]
 
     def is_anchor(self, i: int) -> bool:
-        return self.ops[i]["k"] in ANCHORS and self.ops[i].get("p", -1) < 0
+        op = self.ops[i]
+        if op.get("p", -1) >= 0:
+            return False
+        if self.plain:
+            return op["k"] not in ("Input", "ConstantOp") and i not in self.fused_products
+        return op["k"] in ANCHORS
+
+    # One launch per op (the baseline form): every op that is not a source gets
+    # a level of its own and its value goes through memory.  Ops that share
+    # state stay together: a loop with its body and reductions, a regression
+    # or an order-statistic window with its readers, an accumulator group.
+    def _assign_plain(self):
+        ops, lv = self.ops, self.lv
+        # a product contracted into its adder is recomputed by the adder
+        self.fused_products = {prod for _, (_, prod) in contraction.plan(ops).items()}
+        unit_of: Dict[int, int] = {}
+        for i, op in enumerate(ops):
+            k = op["k"]
+            if op.get("p", -1) >= 0:
+                continue
+            if k in ("Input", "ConstantOp") or i in self.fused_products:
+                continue
+            if k == "ForeachBackWindow":
+                unit_of[i] = self.loop_chain[i][0]
+            elif k in REDUCTIONS:
+                unit_of[i] = self.loop_chain[contraction.reduction_loop(ops, i)][0]
+            elif k in LR_CONS or k in SL_CONS:
+                unit_of[i] = op["in"][0]
+            elif i in self.acc_group:
+                unit_of[i] = ("g", self.acc_group[i])
+            else:
+                unit_of[i] = i
+        members: Dict[object, List[int]] = {}
+        for i, u in unit_of.items():
+            members.setdefault(u, []).append(i)
+        for lp, chain in self.loop_chain.items():
+            if chain[0] == lp:
+                for c in chain:
+                    members[chain[0]] += [j for j in self.body(c) if j not in members[chain[0]]]
+        seq = lambda u: (isinstance(u, tuple) or ops[u]["k"] in SEQ)  # noqa: E731
+        ext: Dict[object, Set[int]] = {}
+        for u, mem in members.items():
+            ms = set(mem)
+            e = set()
+            stack = [x for j in mem if ops[j]["k"] != "Accumulator" for x in ops[j]["in"]]
+            while stack:
+                x = stack.pop()
+                if x in ms:
+                    continue
+                if x in self.fused_products:
+                    stack.extend(ops[x]["in"])
+                elif x in unit_of and unit_of[x] != u:
+                    e.add(x)
+            ext[u] = e
+        done: Dict[object, int] = {}
+        cur = -1
+        pending = sorted(members, key=lambda u: max(members[u]))
+        while pending:
+            progress = False
+            for u in list(pending):
+                if any(unit_of[x] not in done for x in ext[u]):
+                    continue
+                L = cur + 1
+                if seq(u) != (L % 2 == 1):
+                    L += 1
+                cur = L
+                done[u] = L
+                for j in members[u]:
+                    lv[j] = L
+                pending.remove(u)
+                progress = True
+            if not progress:
+                raise Unsupported("plain form: cyclic units")
+        self.levels = sorted(set(done.values())) or [0]
+        self.final = max(self.levels)
 
     def is_source(self, i: int) -> bool:
         return self.ops[i]["k"] in ("Input", "ConstantOp")
@@ -385,7 +463,7 @@ class LeveledGen(StageGen):
 
     def __init__(self, spec: dict, si: int, tag: str):
         super().__init__(spec, si, tag)
-        self.plan = StagePlan(self.ops)
+        self.plan = StagePlan(self.ops, plain=spec.get("form") == "plain")
         self.fplan = contraction.plan(self.ops)
         self.cur_level = None
         self.cur_comp: Set[int] = set()

@@ -25,6 +25,7 @@ CASES = [
     ("alpha158_fast_f32", "alpha158_fast", 64, 300, 0.005, 0),
     ("alpha158_fast_f32", "alpha158_fast", 61, 260, 0.0, 40),
     ("alpha101_fast_f32", "alpha101_fast", 64, 260, 0.005, 0),
+    ("alpha158_plain_f32", "alpha158_plain", 64, 300, 0.005, 0),
 ]
 
 _programs = {}
