@@ -145,6 +145,45 @@ def cpu_reference(workload: dict, steps: int, warmup: int, seconds_target: float
             "s_per_step": dt}
 
 
+def serving(nsess=256, steps=30, seed=3):
+    """Stream serving of the Alpha101 stream module: `nsess` sessions of
+    log-uniform size in [100, 5000] stocks in one pool; every step all
+    sessions submit one tick through the request loop and wait for it.
+    Returns the per-tick latency (submit to result in the pinned host table)
+    percentiles and the throughput."""
+    from kunquant_gb300 import runner as kr
+    from kunquant_gb300 import serve
+    mod = kr.Library.predefined("alpha101_stream_f32").getModule("alpha101_stream")
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(np.log(100), np.log(5000), nsess)).astype(int)
+    cap = int(sizes.sum())
+    ex = kr.createSingleThreadExecutor()
+    pool = serve.ServePool(ex, mod, capacity_stocks=cap, max_sessions=nsess, max_session_stocks=5000)
+    sess = [pool.open(int(n)) for n in sizes]
+    names = mod.getInputNames()
+    base = rng.uniform(10, 100, cap).astype(np.float32)
+    warm = 10
+    for st in range(steps + warm):
+        for s in sess:
+            row = base[s.column:s.column + s.num_stocks] * np.float32(1 + 0.001 * st)
+            for k in names:
+                s.inputs[k][:] = row
+        pool.submit_all(sess)
+        for s in sess:
+            s.wait(60000)
+        if st == warm - 1:
+            pool.take_latencies()
+            t0 = time.perf_counter()
+    el = time.perf_counter() - t0
+    lat, sz = pool.take_latencies()
+    pool.shutdown()
+    return {"module": "alpha101_stream_f32", "sessions": nsess, "stocks": cap, "steps": steps,
+            "sizes": "log-uniform [100, 5000] stocks per session",
+            "p50_tick_us": float(np.percentile(lat, 50)), "p99_tick_us": float(np.percentile(lat, 99)),
+            "stock_ticks_per_s": cap * steps / el, "ms_per_step": el / steps * 1e3,
+            "pool_bytes": serve.pool_bytes(mod, cap)}
+
+
 def stage_bytes(mod_spec, stage_idx, S, T, elem):
     st = mod_spec["stages"][stage_idx]
     return (len(set(st["in"])) + len(st["out"])) * S * T * elem
@@ -161,6 +200,7 @@ def main():
     ap.add_argument("--days", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the stream-serving measurement")
     ap.add_argument("--streams", type=int, default=8, help="CUDA streams for concurrent stages")
     args = ap.parse_args()
     wl = dict(WORKLOADS[args.workload])
@@ -278,6 +318,9 @@ def main():
         e2e = {"value": world * S * T / dt, "unit": "stock-days/s",
                "h2d_bytes_per_step": wl["n_inputs"] * S * T * elem,
                "d2h_bytes_per_step": len(host_out) * S * T * elem, "ms_per_step": dt * 1e3}
+    serve_line = None
+    if rank == 0 and not args.no_serve:
+        serve_line = serving()
     cpu = None
     if rank == 0 and not args.no_cpu:
         ref = cpu_reference(wl, 2, 1, seconds_target=12.0)
@@ -287,6 +330,7 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": config, "roofline": roofline, "cpu_baseline": cpu,
+                "serving": serve_line,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
                 "stage_ms": {str(k): round(v, 4) for k, v in sorted(avg.items(), key=lambda x: -x[1])[:8]}}
         print(json.dumps(line))
