@@ -157,6 +157,28 @@ int kunModuleNumStages(KunModuleHandle m);
 KunStatus kunStreamPushDataDevice(KunStreamContextHandle context, size_t handle, const void *device_buffer);
 const void *kunStreamGetCurrentBufferDevice(KunStreamContextHandle context, size_t handle);
 KunStatus kunStreamRunEx(KunStreamContextHandle context, int synchronize);
+/* Many universes in one run (GPU extension; the reference runs one runGraph
+ * per universe): `njobs` jobs of module m, each with its own buffer map (device
+ * memory), stock count and time range.  Time-series stages run each kernel
+ * once over the tiles of all jobs; the others run job by job.  Waits for the
+ * work before returning. */
+KunStatus kunRunGraphBatch(KunExecutorHandle exec, KunModuleHandle m, int njobs,
+                           const KunBufferNameMapHandle *buffers, const size_t *num_stocks,
+                           const size_t *total_time, const size_t *cur_time, const size_t *length,
+                           int synchronize);
+/* Autotuner (GPU extension): time candidate launch shapes (time tile x
+ * threads per block) of every time-series stage on these jobs and keep the
+ * fastest per stage; the executor then uses them for this module in
+ * kunRunGraphBatch and kunRunGraphEx.  Computes the jobs' outputs on the way.
+ * Returns the number of stages tuned, -1 on error. */
+int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle m, int njobs, const KunBufferNameMapHandle *buffers,
+                    const size_t *num_stocks, const size_t *total_time, const size_t *cur_time,
+                    const size_t *length, int reps);
+/* Tuned shape of one stage (kernel count, 0 if untuned) and clearing it. */
+int kunExecutorTunedShape(KunExecutorHandle exec, KunModuleHandle m, int stage, int32_t *tile, int32_t *block,
+                          int cap);
+KunStatus kunExecutorClearTuning(KunExecutorHandle exec);
+
 /* Batch run that allocates no device memory; no counterpart in the reference.
  * For callers that cannot call cudaMalloc (an allocator-owning host process,
  * code between allocator checkpoints): temporaries and scratch come from a

@@ -72,7 +72,8 @@ def runtime_path() -> str:
 
 def build_runtime(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    srcs = [os.path.join(CSRC, f) for f in ("kun_runtime.cu", "kun_stream.cu", "kun_serve.cu", "kun_noalloc.cu")]
+    srcs = [os.path.join(CSRC, f) for f in ("kun_runtime.cu", "kun_stream.cu", "kun_serve.cu", "kun_batch.cu",
+                                            "kun_noalloc.cu")]
     srcs = [s for s in srcs if os.path.exists(s)]
     lib = runtime_path()
     digest = _hash(srcs + _headers(), " ".join(COMMON_FLAGS) + ARCH)

@@ -99,6 +99,9 @@ class StageGen:
         self.scratch: Dict[int, int] = {}    # WTO op index -> scratch slot
         self.lines: List[str] = []
         self.blocking = spec["blocking_len"]
+        # set by generators whose stages support grouped launches and tuning
+        self.kernel_info = None
+        self.num_kernels_override = None
 
     # ------------------------------------------------------------ helpers
     def slot(self, bid: int) -> int:
@@ -479,7 +482,8 @@ extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
             src, launch = self.gen_ts()
         else:
             src, launch = self.gen_xsec()
-        return src + launch, len(self.scratch), max(1, launch.count("<<<"))
+        nk = self.num_kernels_override or max(1, launch.count("<<<"))
+        return src + launch, len(self.scratch), nk
 
 
 def stage_generator(spec: dict, si: int, tag: str, mode: str = "leveled") -> StageGen:
@@ -539,6 +543,7 @@ template <> struct LogTables<{T}> {{
     state_i = [0] * n_stages
     init_fn = ["nullptr"] * n_stages
     extern_init = []
+    kinfo: Dict[int, List[int]] = {}
     files: List[List[str]] = []
     cur: List[str] = []
     for si in range(n_stages):
@@ -550,6 +555,8 @@ template <> struct LogTables<{T}> {{
         if getattr(g, "has_init", False):
             init_fn[si] = f"kst_{tag}_{si}_init"
             extern_init.append(si)
+        if g.kernel_info:
+            kinfo[si] = g.kernel_info
         cur.append(src)
         if len(cur) >= stages_per_file:
             files.append(cur)
@@ -567,6 +574,10 @@ template <> struct LogTables<{T}> {{
         lines.append(f'extern "C" int kst_{tag}_{si}_launch(const KunGpuStageArgs*, void*);')
     for si in extern_init:
         lines.append(f'extern "C" int kst_{tag}_{si}_init(const KunGpuStageArgs*, void*);')
+    for si, ki in kinfo.items():
+        lines.append(f'extern "C" size_t kst_{tag}_{si}_prepare(const KunGpuStageArgs*, int, void*);')
+        lines.append(f'extern "C" int kst_{tag}_{si}_launch_group(const KunGpuStageArgs*, int, const void*, void*);')
+        lines.append(f"static const int32_t st{si}_kinfo[] = {{{', '.join(str(v) for v in ki)}}};")
     for si, st in enumerate(spec["stages"]):
         for key in ("in", "out", "deps"):
             vals = st.get(key, []) or []
@@ -579,7 +590,9 @@ template <> struct LogTables<{T}> {{
         lines.append(f"  {{{_c_str(st['name'][:200])}, {kinds[st['kind']]}, {len(st['in'])}, st{si}_in, "
                      f"{len(st['out'])}, st{si}_out, {len(st.get('deps', []))}, st{si}_deps, "
                      f"{st.get('pending', 0)}, {scratch_counts[si]}, 0, kst_{tag}_{si}_launch, {kernel_counts[si]}, "
-                     f"{state_t[si]}, {state_i[si]}, {init_fn[si]}}},")
+                     f"{state_t[si]}, {state_i[si]}, {init_fn[si]}, "
+                     + (f"st{si}_kinfo, kst_{tag}_{si}_prepare, kst_{tag}_{si}_launch_group}},"
+                        if si in kinfo else "nullptr, nullptr, nullptr},"))
     lines.append("};")
     bk = {"INPUT": "KUN_BUF_INPUT", "OUTPUT": "KUN_BUF_OUTPUT", "TEMP": "KUN_BUF_TEMP"}
     lines.append(f"static const KunGpuBufferDesc buffers_{tag}[] = {{")

@@ -147,6 +147,26 @@ template <typename T> __device__ __forceinline__ T kexpk(T x) {
     return res;
 }
 
+// ---------------- grouped launches
+// One launch of a stage kernel over several jobs (universes): flat block g
+// belongs to job j when off[j] <= g < off[j+1].  Passed by value.
+#ifndef KUN_MAX_GROUP
+#define KUN_MAX_GROUP 256
+#endif
+struct TileTable {
+    int njobs;
+    int off[KUN_MAX_GROUP + 1];
+};
+__device__ __forceinline__ int tile_job(const TileTable &tt, int g) {
+    int lo = 0, hi = tt.njobs - 1;
+    while (lo < hi) {
+        const int m = (lo + hi + 1) >> 1;
+        if (tt.off[m] <= g) lo = m;
+        else hi = m - 1;
+    }
+    return lo;
+}
+
 // ---------------- compensated fp32 ("double-float") running sums
 // A value hi + lo of two floats (|lo| <= ulp(hi)/2) carries about 48 bits.
 // Sums use Knuth's error-free TwoSum on both parts followed by two

@@ -11,7 +11,7 @@
 extern "C" {
 #endif
 
-#define KUN_GPU_MODULE_ABI 0x6b470005ull
+#define KUN_GPU_MODULE_ABI 0x6b470006ull
 
 typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
 typedef enum { KUN_BUF_INPUT = 0, KUN_BUF_OUTPUT = 1, KUN_BUF_TEMP = 2 } KunGpuBufferKind;
@@ -57,9 +57,20 @@ typedef struct {
      * fields above are upper bounds that size the grids, so one captured
      * graph serves any batch of segments within those bounds. */
     const int32_t *seg_count;
+    /* optional per-kernel launch shape of a time-series stage (num_kernels
+     * entries, 0 = default): time tile in rows (a multiple of 4) and threads
+     * per block (at most 128) */
+    const int32_t *tune_tile;
+    const int32_t *tune_block;
 } KunGpuStageArgs;
 
 typedef int (*KunGpuLaunchFn)(const KunGpuStageArgs *args, void *cuda_stream);
+/* grouped launches over `njobs` jobs (args[0..njobs)): prepare() writes the
+ * jobs' parameter blocks to `host` (when not NULL) and returns their size;
+ * launch_group() runs every kernel of the stage once over all jobs, reading
+ * the blocks from device memory `dev` */
+typedef size_t (*KunGpuPrepareFn)(const KunGpuStageArgs *args, int32_t njobs, void *host);
+typedef int (*KunGpuGroupLaunchFn)(const KunGpuStageArgs *args, int32_t njobs, const void *dev, void *cuda_stream);
 
 typedef struct {
     const char *name;
@@ -80,6 +91,11 @@ typedef struct {
     int32_t state_t_vars;      /* float/double arrays of num_stocks */
     int32_t state_i_vars;      /* int32 arrays of num_stocks */
     KunGpuLaunchFn init;
+    /* time-series stages with grouped launches: per kernel, default time
+     * tile << 1 (or number of scan roles << 1) | 1 for a scan kernel */
+    const int32_t *kernel_info;
+    KunGpuPrepareFn prepare;
+    KunGpuGroupLaunchFn launch_group;
 } KunGpuStageDesc;
 
 typedef struct {

@@ -261,6 +261,11 @@ static KunStatus enqueue_stages(Executor *ex, const KunGpuModuleDesc *m, const P
         a.start = cur_time;
         a.length = length;
         a.error_flag = ex->d_error;
+        auto tn = ex->tuning.find((const void *)m);
+        if (tn != ex->tuning.end() && si < (int)tn->second.size() && !tn->second[si].tile.empty()) {
+            a.tune_tile = tn->second[si].tile.data();
+            a.tune_block = tn->second[si].block.data();
+        }
         int rc = s.launch(&a, (void *)st);
         launches += s.num_kernels > 0 ? s.num_kernels : 1;
         if (rc != 0) {
@@ -522,6 +527,7 @@ void destroy_executor(Executor *ex) {
         cudaStreamSynchronize(cs);
         cudaStreamDestroy(cs);
     }
+    if (ex->group_host) cudaFreeHost(ex->group_host);
     for (auto e : ex->copy_ev) cudaEventDestroy(e);
     for (auto e : ex->copy_done) cudaEventDestroy(e);
     delete ex;

@@ -99,6 +99,16 @@ struct Executor {
     // bridged to the caller's stream with these events
     bool has_user_stream = false;
     cudaEvent_t bridge_in = nullptr, bridge_out = nullptr;
+    // tuned launch shapes per module and stage (time tile, threads per
+    // block, per kernel); empty vectors mean the generated defaults
+    struct StageTune {
+        std::vector<int32_t> tile, block;
+    };
+    std::map<const void *, std::vector<StageTune>> tuning;
+    // pinned host and device staging of grouped-launch parameter blocks
+    void *group_host = nullptr;
+    Arena group_dev;
+    size_t group_host_bytes = 0;
     // copy streams for device-to-host output copies overlapping the stages
     std::vector<cudaStream_t> copy_streams;
     std::vector<cudaEvent_t> copy_ev;    // per stage: its outputs are ready

@@ -961,10 +961,13 @@ class LeveledGen(StageGen):
         self.mats = set(mats)
         for j in mats:
             self.scratch[j] = len(self.scratch)
-        srcs, calls = [], []
+        srcs, calls, kinfo = [], [], []
+        knames = []
+        pstruct = f"P_{self.kname}"
         for ki, kd in enumerate(ks):
             L = kd["level"]
             kname = f"{self.kname}_L{L}_{ki}"
+            knames.append(kname)
             decl: List[str] = []
             seen: Set[int] = set()
             self.lines = []
@@ -982,8 +985,10 @@ class LeveledGen(StageGen):
                 states = [self._state_decl(i) for i in sls]
                 wmax = max([ops[i]["window"] for i in sls] + [0])
                 chunk = max(PAR_CHUNK, 4 * wmax)
-                self.lines.append(f"  const long long t0 = (long long)blockIdx.y * {chunk};")
-                self.lines.append(f"  const long long t1 = t0 + {chunk} < length ? t0 + {chunk} : length;")
+                # the time tile is a launch parameter (tunable, a multiple of 4)
+                self.lines.append(f"  const long long tile = P.tile[{ki}];")
+                self.lines.append("  const long long t0 = (long long)by * tile;")
+                self.lines.append("  const long long t1 = t0 + tile < length ? t0 + tile : length;")
                 for sd in states:
                     self.lines.append(f"  {sd}")
                 if sls:
@@ -1007,10 +1012,10 @@ class LeveledGen(StageGen):
                     self.lines.append(f"  for (long long t = t0; t < t1; t += {VEC_U}) {{")
                     self._emit_par_vec(comp, vr, stores, loops, VEC_U, "    ")
                 self.lines.append("  }")
-                grid_y = f"(unsigned)((a->length + {chunk} - 1) / {chunk})"
+                kinfo.append((chunk, 0))
             else:
                 roles = kd["roles"]
-                self.lines.append("  switch (blockIdx.y) {")
+                self.lines.append("  switch (by) {")
                 for ri, r in enumerate(roles):
                     self.lines.append(f"  case {ri}: {{")
                     # each role declares only the series it touches, so the
@@ -1031,30 +1036,114 @@ class LeveledGen(StageGen):
                     self.lines.append("  } break;")
                 self.lines.append("  default: break;")
                 self.lines.append("  }")
-                grid_y = str(len(roles))
+                kinfo.append((len(roles), 1))
+            # the body takes its block coordinates as arguments, so the same
+            # code serves a launch of one job and a grouped launch of many
             srcs.append(f"""
-__global__ void __launch_bounds__(KUN_TS_THREADS) {kname}(const P_{self.kname} P) {{
+__device__ __forceinline__ void {kname}_body(const {pstruct}& P, const int bx, const int by) {{
   const long long S = P.S;
-  const long long s = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long s = (long long)bx * blockDim.x + threadIdx.x;
   if (s >= S) return;
   const long long total_time = P.total_time, start = P.start, length = P.length;
   (void)total_time; (void)start;
 {chr(10).join(decl)}
 {chr(10).join(self.lines)}
 }}
+__global__ void __launch_bounds__(KUN_TS_THREADS) {kname}(const {pstruct} P) {{
+  {kname}_body(P, blockIdx.x, blockIdx.y);
+}}
+__global__ void __launch_bounds__(KUN_TS_THREADS) {kname}_grp(const {pstruct}* __restrict__ jobs, const kun::TileTable tt) {{
+  const int j = kun::tile_job(tt, blockIdx.x);
+  const {pstruct}& P = jobs[j];
+  const int local = (int)blockIdx.x - tt.off[j];
+  const int gx = (int)((P.S + blockDim.x - 1) / blockDim.x);
+  {kname}_body(P, local % gx, local / gx);
+}}
 """)
-            calls.append(f"  {kname}<<<dim3((unsigned)((a->num_stocks + KUN_TS_THREADS - 1) / KUN_TS_THREADS), "
-                         f"{grid_y}), KUN_TS_THREADS, 0, (cudaStream_t)stream>>>(P);\n"
-                         f"  if (cudaError_t e = cudaGetLastError()) return (int)e;")
         nslots = max(1, len(self.slots))
         nscr = max(1, len(self.scratch))
-        pstruct = f"P_{self.kname}"
+        nk = len(ks)
         head = f"""
 struct {pstruct} {{
   void* p[{nslots}];
   void* w[{nscr}];
   long long S, total_time, start, length;
+  int tile[{nk}];
 }};
 """
-        launch = self.launcher(pstruct, "\n".join(calls))
+        self.kernel_info = [(d << 1) | sc for d, sc in kinfo]
+        self.num_kernels_override = nk
+        # per kernel: time tile (or roles) and block size, from the tuning
+        # arrays when given
+        sel = []
+        for k, (d, sc) in enumerate(kinfo):
+            sel.append(f"  const int blk{k} = (a->tune_block && a->tune_block[{k}] > 0) ? a->tune_block[{k}] : KUN_TS_THREADS;")
+            if not sc:
+                sel.append(f"  P.tile[{k}] = (a->tune_tile && a->tune_tile[{k}] > 0) ? a->tune_tile[{k}] : {d};")
+            else:
+                sel.append(f"  P.tile[{k}] = 0;")
+        for k, (d, sc) in enumerate(kinfo):
+            gy = str(d) if sc else f"(unsigned)((a->length + P.tile[{k}] - 1) / P.tile[{k}])"
+            calls.append(f"  {knames[k]}<<<dim3((unsigned)((a->num_stocks + blk{k} - 1) / blk{k}), {gy}), blk{k}, 0, "
+                         f"(cudaStream_t)stream>>>(P);\n"
+                         f"  if (cudaError_t e = cudaGetLastError()) return (int)e;")
+        launch = self.launcher(pstruct, "\n".join(sel + calls))
+        launch += self._group_launcher(pstruct, knames, kinfo)
         return head + "".join(srcs), launch
+
+    def _group_launcher(self, pstruct: str, knames: List[str], kinfo) -> str:
+        """prepare(): the parameter blocks of n jobs; launch_group(): every
+        kernel of the stage once over all jobs' tiles."""
+        fill = "\n".join(f"    P.p[{sl}] = a->buffers[{bid}];" for bid, sl in self.slots.items())
+        fillw = "\n".join(f"    P.w[{sc}] = a->scratch[{sc}];" for sc in range(len(self.scratch)))
+        tiles = []
+        for k, (d, sc) in enumerate(kinfo):
+            if sc:
+                tiles.append(f"    P.tile[{k}] = 0;")
+            else:
+                tiles.append(f"    P.tile[{k}] = (a->tune_tile && a->tune_tile[{k}] > 0) ? a->tune_tile[{k}] : {d};")
+        launches = []
+        for k, (d, sc) in enumerate(kinfo):
+            gy = str(d) if sc else f"(a->length + tile - 1) / tile"
+            tl = "0" if sc else f"(a->tune_tile && a->tune_tile[{k}] > 0) ? a->tune_tile[{k}] : {d}"
+            launches.append(f"""  {{
+    const int blk = (args[0].tune_block && args[0].tune_block[{k}] > 0) ? args[0].tune_block[{k}] : KUN_TS_THREADS;
+    kun::TileTable tt;
+    tt.njobs = njobs;
+    long long total = 0;
+    for (int j = 0; j < njobs; ++j) {{
+      const KunGpuStageArgs* a = &args[j];
+      const long long tile = {tl};
+      (void)tile;
+      tt.off[j] = (int)total;
+      if (a->num_stocks > 0 && a->length > 0) total += ((a->num_stocks + blk - 1) / blk) * (long long)({gy});
+    }}
+    tt.off[njobs] = (int)total;
+    if (total > 0x7fffffffLL) return (int)cudaErrorInvalidValue;
+    if (total > 0) {{
+      {knames[k]}_grp<<<(unsigned)total, blk, 0, (cudaStream_t)stream>>>((const {pstruct}*)dev, tt);
+      if (cudaError_t e = cudaGetLastError()) return (int)e;
+    }}
+  }}""")
+        return f"""
+extern "C" size_t {self.kname}_prepare(const KunGpuStageArgs* args, int njobs, void* host) {{
+  if (host) {{
+    for (int j = 0; j < njobs; ++j) {{
+      const KunGpuStageArgs* a = &args[j];
+      {pstruct}& P = (({pstruct}*)host)[j];
+{fill}
+{fillw}
+      P.S = a->num_stocks; P.total_time = a->total_time; P.start = a->start; P.length = a->length;
+{chr(10).join(tiles)}
+    }}
+  }}
+  return sizeof({pstruct}) * (size_t)njobs;
+}}
+
+extern "C" int {self.kname}_launch_group(const KunGpuStageArgs* args, int njobs, const void* dev, void* stream) {{
+  if (njobs <= 0) return 0;
+  if (njobs > KUN_MAX_GROUP) return (int)cudaErrorInvalidValue;
+{chr(10).join(launches)}
+  return 0;
+}}
+"""

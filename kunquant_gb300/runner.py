@@ -473,3 +473,96 @@ class StreamContext:
 def streamBytesPerStock(mod: Module) -> int:
     """Device bytes one stock of a stream module occupies (rings + states)."""
     return int(runtime().kunStreamBytesPerStock(mod.handle))
+
+
+def _batch_maps(mod: Module, inputs_list, outputs_list, cur_time, length):
+    """Buffer maps and shapes of a list of jobs (torch CUDA tensors, [T][S])."""
+    import torch
+    L = runtime()
+    dt = torch.float32 if mod.dtype == np.float32 else torch.float64
+    maps, S, TT, CT, LN, outs = [], [], [], [], [], []
+    for j, inp in enumerate(inputs_list):
+        if not inp or not all(_is_torch_cuda(v) for v in inp.values()):
+            raise KunError("runGraphBatch takes torch CUDA tensors")
+        T, n = next(iter(inp.values())).shape
+        ln = (T - cur_time) if length is None else length
+        o = dict(outputs_list[j]) if outputs_list else {}
+        m = L.kunCreateBufferNameMap()
+        maps.append(m)
+        for k, v in inp.items():
+            _check_contiguous(v, k, (T, n), mod.dtype, True)
+            L.kunSetBufferNameMap(m, k.encode(), ctypes.c_void_p(v.data_ptr()))
+        for k in mod.getOutputNames():
+            if k not in o:
+                o[k] = torch.empty((ln, n), dtype=dt, device=next(iter(inp.values())).device)
+            L.kunSetBufferNameMap(m, k.encode(), ctypes.c_void_p(o[k].data_ptr()))
+        outs.append(o)
+        S.append(n), TT.append(T), CT.append(cur_time), LN.append(ln)
+    arr = lambda xs, t: (t * len(xs))(*xs)  # noqa: E731
+    return (maps, (ctypes.c_void_p * len(maps))(*maps), arr(S, ctypes.c_size_t), arr(TT, ctypes.c_size_t),
+            arr(CT, ctypes.c_size_t), arr(LN, ctypes.c_size_t), outs)
+
+
+def _batch_sigs(L):
+    if not getattr(L, "_batch_sigs", False):
+        vp, i32 = ctypes.c_void_p, ctypes.c_int
+        szp = ctypes.POINTER(ctypes.c_size_t)
+        L.kunRunGraphBatch.restype = i32
+        L.kunRunGraphBatch.argtypes = [vp, vp, i32, ctypes.POINTER(vp), szp, szp, szp, szp, i32]
+        L.kunExecutorTune.restype = i32
+        L.kunExecutorTune.argtypes = [vp, vp, i32, ctypes.POINTER(vp), szp, szp, szp, szp, i32]
+        L.kunExecutorTunedShape.restype = i32
+        L.kunExecutorTunedShape.argtypes = [vp, vp, i32, ctypes.POINTER(ctypes.c_int32),
+                                            ctypes.POINTER(ctypes.c_int32), i32]
+        L.kunExecutorClearTuning.restype = i32
+        L.kunExecutorClearTuning.argtypes = [vp]
+        L._batch_sigs = True
+    return L
+
+
+def runGraphBatch(exec: Executor, mod: Module, inputs_list, cur_time: int = 0, length: Optional[int] = None,
+                  outputs_list=None):
+    """Run many universes of one module in one call (GPU extension): each
+    element of ``inputs_list`` is one universe's inputs (torch CUDA tensors,
+    [T][S], any S and T).  Returns the list of output dicts."""
+    import torch
+    L = _batch_sigs(runtime())
+    maps, cmaps, S, TT, CT, LN, outs = _batch_maps(mod, inputs_list, outputs_list, cur_time, length)
+    try:
+        L.kunExecutorSetStream(exec.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+        rc = L.kunRunGraphBatch(exec.handle, mod.handle, len(maps), cmaps, S, TT, CT, LN, 1)
+        L.kunExecutorClearStream(exec.handle)
+        _check(rc)
+    finally:
+        for m in maps:
+            L.kunDestoryBufferNameMap(m)
+    return outs
+
+
+def tune(exec: Executor, mod: Module, inputs_list, cur_time: int = 0, length: Optional[int] = None, reps: int = 2):
+    """Autotune the launch shapes (time tile, threads per block) of every
+    time-series stage of ``mod`` on these universes; the executor keeps them
+    for later runs of the module.  Returns the number of stages tuned."""
+    import torch
+    L = _batch_sigs(runtime())
+    maps, cmaps, S, TT, CT, LN, _ = _batch_maps(mod, inputs_list, None, cur_time, length)
+    try:
+        torch.cuda.synchronize()
+        n = L.kunExecutorTune(exec.handle, mod.handle, len(maps), cmaps, S, TT, CT, LN, reps)
+    finally:
+        for m in maps:
+            L.kunDestoryBufferNameMap(m)
+    if n < 0:
+        raise KunError(_err() or "tuning failed")
+    return n
+
+
+def tunedShape(exec: Executor, mod: Module, stage: int):
+    """(time tiles, threads per block) chosen for one stage, or None."""
+    L = _batch_sigs(runtime())
+    t = (ctypes.c_int32 * 64)()
+    b = (ctypes.c_int32 * 64)()
+    n = L.kunExecutorTunedShape(exec.handle, mod.handle, stage, t, b, 64)
+    if n <= 0:
+        return None
+    return list(t[:n]), list(b[:n])
