@@ -179,6 +179,20 @@ int kunExecutorTunedShape(KunExecutorHandle exec, KunModuleHandle m, int stage, 
                           int cap);
 KunStatus kunExecutorClearTuning(KunExecutorHandle exec);
 
+/* corrWith / RankCorrWith (GPU extension; the reference has them in C++ and
+ * Python, cpp/Kun/CorrWith.hpp): for each of n inputs, out[k][t] = the
+ * correlation across stocks of inputs[k] row t with corr_with row t (with
+ * rank_inputs, of the input's cross-sectional rank).  Device memory; layout
+ * 1 = TS [T][S], 0 = STs [S/8][T][8] (TS only with rank_inputs). */
+KunStatus kunCorrWith(KunExecutorHandle exec, int n, const float *const *inputs, const float *corr_with,
+                      float *const *outs, size_t num_stocks, size_t num_time, int layout, int rank_inputs);
+/* aggregrate (GPU extension, cpp/Kun/Aggregration.cpp; the reference's
+ * spelling): per stock, reductions over runs of equal consecutive labels.
+ * outs[k*7 + kind], kind = sum, min, max, first, last, count, mean (NULL to
+ * skip), each [groups][S]; dtype 0 float, 1 double; device memory. */
+KunStatus kunAggregrate(KunExecutorHandle exec, int n, const void *const *inputs, const void *const *labels,
+                        void *const *outs, size_t num_stocks, size_t length, int dtype);
+
 /* Batch run that allocates no device memory; no counterpart in the reference.
  * For callers that cannot call cudaMalloc (an allocator-owning host process,
  * code between allocator checkpoints): temporaries and scratch come from a

@@ -30,9 +30,11 @@ COMMON_FLAGS = ["-gencode", f"arch=compute_{ARCH},code=sm_{ARCH}", "-O3", "-line
 # call kfma() explicitly (see contraction.py)
 MODULE_FLAGS = COMMON_FLAGS + ["-fmad=false"]
 
+# built by build_all(); the other forms (alpha158_fast_f32, alpha101_fast_f32,
+# alpha158_comp_f32, alpha158_acc64_f32, alpha158_plain_f32) are built on
+# first use by predefined_library()
 PREDEFINED = ["alpha101_f32", "alpha158_f32", "alpha101_f64", "alpha158_f64", "alpha101_stream_f32",
-              "alpha158_stream_f32", "alpha158_fast_f32", "alpha101_fast_f32", "alpha158_acc64_f32",
-              "alpha158_comp_f32", "alpha158_plain_f32"]
+              "alpha158_stream_f32"]
 
 
 def _hash(paths: Iterable[str], extra: str) -> str:
@@ -73,7 +75,7 @@ def runtime_path() -> str:
 def build_runtime(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     srcs = [os.path.join(CSRC, f) for f in ("kun_runtime.cu", "kun_stream.cu", "kun_serve.cu", "kun_batch.cu",
-                                            "kun_noalloc.cu")]
+                                            "kun_util.cu", "kun_noalloc.cu")]
     srcs = [s for s in srcs if os.path.exists(s)]
     lib = runtime_path()
     digest = _hash(srcs + _headers(), " ".join(COMMON_FLAGS) + ARCH)

@@ -566,3 +566,115 @@ def tunedShape(exec: Executor, mod: Module, stage: int):
     if n <= 0:
         return None
     return list(t[:n]), list(b[:n])
+
+
+_AGG_KINDS = ["sum", "min", "max", "first", "last", "count", "mean"]
+
+
+def _to_device(a):
+    """(torch CUDA tensor, was_numpy) of an array."""
+    import torch
+    if _is_torch_cuda(a):
+        return a, False
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda(), True
+
+
+def corrWith(exec: Executor, inputs, corr_with, outs, layout: str = "TS", rank_inputs: bool = False):
+    """Cross-sectional correlation of every row of each input with the same
+    row of ``corr_with`` (``cpp/Python/PyBinding.cpp:396-447``): ``outs[k][t]``.
+    numpy arrays or torch CUDA tensors; fp32."""
+    import torch
+    if layout not in ("TS", "STs"):
+        raise KunError("Unknown layout" + layout)
+    if len(inputs) != len(outs):
+        raise KunError("number of inputs and outputs should match")
+    L = runtime()
+    if not getattr(L, "_util_sigs", False):
+        vp, sz, i32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+        L.kunCorrWith.restype = i32
+        L.kunCorrWith.argtypes = [vp, i32, ctypes.POINTER(vp), vp, ctypes.POINTER(vp), sz, sz, i32, i32]
+        L.kunAggregrate.restype = i32
+        L.kunAggregrate.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), sz, sz, i32]
+        L._util_sigs = True
+    y, _ = _to_device(corr_with)
+    if y.dtype != torch.float32:
+        raise KunError("Expecting float buffer at corr_with")
+    if layout == "TS":
+        T, S = y.shape
+    else:
+        nb, T, blk = y.shape
+        S = nb * blk
+    dev_in = []
+    for i, a in enumerate(inputs):
+        d, _ = _to_device(a)
+        if tuple(d.shape) != tuple(y.shape) or d.dtype != torch.float32:
+            raise KunError(f"Bad shape at buffer_{i}")
+        dev_in.append(d.contiguous())
+    dev_out = [torch.empty(T, dtype=torch.float32, device=y.device) for _ in outs]
+    pin = (ctypes.c_void_p * len(dev_in))(*[d.data_ptr() for d in dev_in])
+    pout = (ctypes.c_void_p * len(dev_out))(*[d.data_ptr() for d in dev_out])
+    L.kunExecutorSetStream(exec.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    rc = L.kunCorrWith(exec.handle, len(dev_in), pin, ctypes.c_void_p(y.contiguous().data_ptr()), pout, S, T,
+                       1 if layout == "TS" else 0, 1 if rank_inputs else 0)
+    L.kunExecutorClearStream(exec.handle)
+    _check(rc)
+    for o, d in zip(outs, dev_out):
+        if _is_torch_cuda(o):
+            o.copy_(d)
+        else:
+            o[...] = d.cpu().numpy()
+
+
+def aggregrate(exec: Executor, inputs, labels, outs):
+    """Per-stock reductions over runs of equal consecutive labels
+    (``cpp/Python/PyBinding.cpp:449-506``; the reference's spelling): for
+    input k ([T][S]) and labels k ([T]), ``outs[k]`` maps any of sum, min, max,
+    first, last, count, mean to a [groups][S] array it fills."""
+    import torch
+    if len(inputs) != len(labels) or len(inputs) != len(outs):
+        raise KunError("number of inputs, labels and outputs should match")
+    if not inputs:
+        return
+    L = runtime()
+    if not getattr(L, "_util_sigs", False):
+        vp, sz, i32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int
+        L.kunCorrWith.restype = i32
+        L.kunCorrWith.argtypes = [vp, i32, ctypes.POINTER(vp), vp, ctypes.POINTER(vp), sz, sz, i32, i32]
+        L.kunAggregrate.restype = i32
+        L.kunAggregrate.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), sz, sz, i32]
+        L._util_sigs = True
+    first, _ = _to_device(inputs[0])
+    dt = first.dtype
+    if dt not in (torch.float32, torch.float64):
+        raise KunError("aggregrate takes float or double buffers")
+    T, S = first.shape
+    keep, pin, plab, pout, back = [], [], [], [], []
+    for k, (a, lab, o) in enumerate(zip(inputs, labels, outs)):
+        d, _ = _to_device(a)
+        lb, _ = _to_device(lab)
+        if tuple(d.shape) != (T, S) or d.dtype != dt or lb.dtype != dt or tuple(lb.shape) != (T,):
+            raise KunError(f"Bad shape at buffer_{k}")
+        d, lb = d.contiguous(), lb.contiguous()
+        keep += [d, lb]
+        pin.append(d.data_ptr())
+        plab.append(lb.data_ptr())
+        row = [None] * 7
+        for name, arr in o.items():
+            if name not in _AGG_KINDS:
+                raise KunError("Unknown aggregration kind: " + name)
+            dev = arr if _is_torch_cuda(arr) else torch.empty(tuple(arr.shape), dtype=dt, device=d.device)
+            if dev.shape[1] != S:
+                raise KunError(f"Bad shape at output_{name}{_AGG_KINDS.index(name)}")
+            keep.append(dev)
+            row[_AGG_KINDS.index(name)] = dev.data_ptr()
+            if not _is_torch_cuda(arr):
+                back.append((arr, dev))
+        pout += row
+    vp = ctypes.c_void_p
+    L.kunExecutorSetStream(exec.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    rc = L.kunAggregrate(exec.handle, len(pin), (vp * len(pin))(*pin), (vp * len(plab))(*plab),
+                         (vp * len(pout))(*pout), S, T, 0 if dt == torch.float32 else 1)
+    L.kunExecutorClearStream(exec.handle)
+    _check(rc)
+    for arr, dev in back:
+        arr[...] = dev.cpu().numpy()

@@ -235,6 +235,36 @@ def predefined_cases():
     }
 
 
+def _utilities():
+    """The reference's aggregrate and corrWith (tests/test_runtime.py shapes:
+    240 rows x 16 stocks, labels = day of a sorted random minute stamp)."""
+    from KunQuant.runner import KunRunner as kr
+    rng = np.random.default_rng(77)
+    ex = kr.createMultiThreadExecutor(3)
+    for dt, tag in ((np.float32, "f32"), (np.float64, "f64")):
+        a = rng.random((240, 16)).astype(dt)
+        b = rng.random((240, 16)).astype(dt)
+        a[17, 3] = np.nan
+        b[100:103, 5] = np.nan
+        days = np.sort(rng.integers(1, 8, 240)).astype(dt)
+        ng = len(np.unique(days))
+        outs = [{k: np.empty((ng, 16), dt) for k in ("sum", "min", "max", "first", "last", "count", "mean")}
+                for _ in range(2)]
+        kr.aggregrate(ex, [a, b], [days, days], outs)
+        out = {f"a_{k}": v for k, v in outs[0].items()}
+        out.update({f"b_{k}": v for k, v in outs[1].items()})
+        _save("util_aggregrate_" + tag, {"utility": "aggregrate"}, {"a": a, "b": b, "labels": days}, out)
+    a = rng.random((24, 40)).astype(np.float32)
+    b = rng.random((24, 40)).astype(np.float32)
+    ret = rng.random((24, 40)).astype(np.float32)
+    o1, o2 = np.empty(24, np.float32), np.empty(24, np.float32)
+    kr.corrWith(ex, [a, b], ret, [o1, o2], "TS")
+    r1, r2 = np.empty(24, np.float32), np.empty(24, np.float32)
+    kr.corrWith(ex, [a, b], ret, [r1, r2], "TS", rank_inputs=True)
+    _save("util_corrwith", {"utility": "corrWith"}, {"a": a, "b": b, "ret": ret},
+          {"a": o1, "b": o2, "rank_a": r1, "rank_b": r2})
+
+
 def main(names):
     from oracle import refkun
     from oracle.build_ref import import_reference
@@ -254,6 +284,8 @@ def main(names):
         data = synth.ohlcv(8, 60, seed=99, nan_frac=0.0)
         out = refkun.run_stream(key, data)
         _save("alpha101_stream_f32", {"predefined": key}, data, out, {"stream": True})
+    if not names or any(n.startswith("util_") for n in names):
+        _utilities()
     for name, (build, cfg, kind) in _graphs().items():
         if names and name not in names:
             continue

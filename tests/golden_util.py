@@ -30,3 +30,9 @@ def is_stream(name):
     """Stream-mode fixtures hold the reference StreamContext's outputs."""
     with gzip.open(os.path.join(GOLDEN, name + ".json.gz"), "rb") as f:
         return bool(json.loads(f.read()).get("stream"))
+
+
+def is_utility(name):
+    """Fixtures of the reference's aggregrate / corrWith utilities."""
+    with gzip.open(os.path.join(GOLDEN, name + ".json.gz"), "rb") as f:
+        return "utility" in json.loads(f.read())["spec"]

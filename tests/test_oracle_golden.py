@@ -44,7 +44,7 @@ def rank_amplified(name):
     return _lookup(RANK_AMPLIFIED, name)
 
 
-BATCH = [n for n in G.names() if not G.is_stream(n)]
+BATCH = [n for n in G.names() if not G.is_stream(n) and not G.is_utility(n)]
 
 
 @pytest.mark.parametrize("name", BATCH)
