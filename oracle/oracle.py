@@ -301,6 +301,34 @@ class OracleProgram:
             self.stages[j].ops = ctypes.cast(arr, ctypes.POINTER(KOOp))
 
     def run(self, inputs, cur_time=0, length=None, num_stocks=None, nthreads=None, outputs=None):
+        """Inputs and outputs in the spec's layouts; the STs layout
+        ([S/L][T][L], Module.hpp / LayoutMappers.hpp:19-22) is converted to
+        and from [T][S] around the computation, which is layout-free."""
+        spec = self.spec
+        L = spec.get("blocking_len", 8)
+        if spec.get("input_layout") == "STs":
+            sv = set(spec.get("single_value_inputs", []))
+            conv = {}
+            for k, a in inputs.items():
+                if k in sv or np.ndim(a) != 3:
+                    conv[k] = a
+                else:
+                    nb, T_, Lb = a.shape
+                    conv[k] = np.ascontiguousarray(np.asarray(a).transpose(1, 0, 2).reshape(T_, nb * Lb))
+            inputs = conv
+        if spec.get("output_layout") == "STs":
+            ts = self._run_ts(inputs, cur_time, length, num_stocks, nthreads, None)
+            out = {}
+            for k, a in ts.items():
+                T_, S_ = a.shape
+                pad = (-S_) % L
+                if pad:
+                    a = np.concatenate([a, np.zeros((T_, pad), a.dtype)], axis=1)
+                out[k] = np.ascontiguousarray(a.reshape(T_, -1, L).transpose(1, 0, 2))
+            return out
+        return self._run_ts(inputs, cur_time, length, num_stocks, nthreads, outputs)
+
+    def _run_ts(self, inputs, cur_time=0, length=None, num_stocks=None, nthreads=None, outputs=None):
         spec = self.spec
         T = None
         S = num_stocks

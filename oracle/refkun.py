@@ -60,7 +60,8 @@ def run_batch(key: str, inputs: dict, cur_time=0, length=None, threads=1):
     """runGraph of the reference on [T][S] inputs; returns {name: [length][S]}."""
     lib, mod = compile_predefined(key)
     from KunQuant.runner import KunRunner as kr
-    T = next(iter(inputs.values())).shape[0]
+    a0 = next(iter(inputs.values()))
+    T = a0.shape[1] if a0.ndim == 3 else a0.shape[0]  # [S/L][T][L] or [T][S]
     if length is None:
         length = T - cur_time
     ex = kr.createSingleThreadExecutor() if threads == 1 else kr.createMultiThreadExecutor(threads)
@@ -122,7 +123,8 @@ def compile_function(key: str, build, modname: str, **cfg_kw):
 
 def run_module(mod, inputs: dict, cur_time=0, length=None, threads=1):
     from KunQuant.runner import KunRunner as kr
-    T = next(iter(inputs.values())).shape[0]
+    a0 = next(iter(inputs.values()))
+    T = a0.shape[1] if a0.ndim == 3 else a0.shape[0]  # [S/L][T][L] or [T][S]
     if length is None:
         length = T - cur_time
     ex = kr.createSingleThreadExecutor() if threads == 1 else kr.createMultiThreadExecutor(threads)

@@ -151,6 +151,12 @@ def _graphs():
         "skiplists_f32": (mk(skiplists), dict(input_layout="TS", output_layout="TS"), "long"),
         "misc_f32": (mk(misc), dict(input_layout="TS", output_layout="TS",
                                     options={"opt_reduce": True}), "ab"),
+        # the reference's default [S/8][T][8] layout in and out
+        "stats_sts_f32": (mk(stats), dict(input_layout="STs", output_layout="STs",
+                                          options={"opt_reduce": True}), "ab_sts"),
+        "rank_sts_f32": (mk(rank029), dict(input_layout="STs", output_layout="STs"), "u24_sts"),
+        "stats_ts_sts_f32": (mk(stats), dict(input_layout="TS", output_layout="STs",
+                                             options={"opt_reduce": True}), "ab"),
     }
 
 
@@ -194,6 +200,9 @@ def _inputs(kind, dtype):
         a = rng.integers(0, 40, size=(600, 8)).astype(dtype) / 4
         a[300:305, 2] = np.nan
         return {"a": a}
+    if kind in ("ab_sts", "u24_sts"):
+        base = _inputs("ab" if kind == "ab_sts" else "u24", dtype)
+        return {k: _to_sts(v) for k, v in base.items()}
     if kind == "stream24":
         return {"a": rng.random((100, 24)).astype(dtype)}
     if kind == "stream_ab":
@@ -203,6 +212,12 @@ def _inputs(kind, dtype):
         a[40, :] = 0.5
         return {"a": a, "b": b}
     raise KeyError(kind)
+
+
+def _to_sts(a, L=8):
+    """[T][S] -> [S/L][T][L]."""
+    T, S = a.shape
+    return np.ascontiguousarray(a.T.reshape(S // L, L, T).transpose(0, 2, 1))
 
 
 def _save(name, spec, inputs, outputs, extra=None):

@@ -36,3 +36,9 @@ def is_utility(name):
     """Fixtures of the reference's aggregrate / corrWith utilities."""
     with gzip.open(os.path.join(GOLDEN, name + ".json.gz"), "rb") as f:
         return "utility" in json.loads(f.read())["spec"]
+
+
+def num_time(inputs):
+    """Rows of a fixture's inputs: [T][S] or STs [S/L][T][L]."""
+    a = next(iter(inputs.values()))
+    return a.shape[1] if a.ndim == 3 else a.shape[0]

@@ -39,7 +39,7 @@ def _module(spec):
 def test_gpu_matches_reference_and_oracle(name):
     spec, inp, ref, meta = G.load(name)
     start = meta.get("cur_time", 0)
-    T = next(iter(inp.values())).shape[0]
+    T = G.num_time(inp)
     ex = kr.createSingleThreadExecutor()
     got = kr.runGraph(ex, _module(spec), inp, start, T - start)
     want = OracleProgram(spec).run(inp, cur_time=start, length=T - start)

@@ -51,7 +51,7 @@ BATCH = [n for n in G.names() if not G.is_stream(n) and not G.is_utility(n)]
 def test_oracle_matches_reference(name):
     spec, inp, ref, meta = G.load(name)
     start = meta.get("cur_time", 0)
-    T = next(iter(inp.values())).shape[0]
+    T = G.num_time(inp)
     out = OracleProgram(spec).run(inp, cur_time=start, length=T - start)
     assert set(out) == set(ref)
     bad = compare_exact(out, ref)
