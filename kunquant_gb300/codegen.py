@@ -445,8 +445,6 @@ extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
         in_user = ["1" if self.is_user_input(o) else "0" for o in ins]
         lay_in = [self.layout_of(o) for o in ins]
         lay_out = self.layout_of(outop)
-        if any(l != "TS" for l in lay_in + [lay_out]):
-            raise RuntimeError("cross-sectional stages support the TS layout only")
         nslots = len(self.slots)
         pstruct = f"P_{self.kname}"
         src = f"""
@@ -455,24 +453,45 @@ struct {pstruct} {{
   long long S, total_time, start, length;
 }};
 """
-        if kind == "rank":
-            call = (f"return kun::launch_rank<{T}>((const {T}*)P.p[{in_slots[0]}] + ({in_user[0]} ? P.start : 0) * P.S, "
-                    f"({T}*)P.p[{out_slot}], P.S, P.length, (cudaStream_t)stream);")
-        elif kind == "scale":
-            call = (f"return kun::launch_scale<{T}>((const {T}*)P.p[{in_slots[0]}] + ({in_user[0]} ? P.start : 0) * P.S, "
-                    f"({T}*)P.p[{out_slot}], P.S, P.length, (cudaStream_t)stream);")
+        # STs operands go through [length][S] scratch copies (the row
+        # kernels read and write [T][S] rows)
+        pre, post = [], []
+        L = self.blocking
+        argin = []
+        for k, (o, sl, lay) in enumerate(zip(ins, in_slots, lay_in)):
+            if lay == "STs":
+                sc = len(self.scratch)
+                self.scratch[("in", k)] = sc
+                rows = "P.total_time" if in_user[k] == "1" else "P.length"
+                row0 = "P.start" if in_user[k] == "1" else "0"
+                pre.append(f"  if (int e = kun::launch_sts_to_ts<{T}>((const {T}*)P.p[{sl}], ({T}*)a->scratch[{sc}], "
+                           f"P.S, {rows}, {row0}, P.length, {L}, (cudaStream_t)stream)) return e;")
+                argin.append(f"(const {T}*)a->scratch[{sc}]")
+            else:
+                argin.append(f"(const {T}*)P.p[{sl}] + ({in_user[k]} ? P.start : 0) * P.S")
+        if lay_out == "STs":
+            sc = len(self.scratch)
+            self.scratch[("out", 0)] = sc
+            argout = f"({T}*)a->scratch[{sc}]"
+            post.append(f"  if (int e = kun::launch_ts_to_sts<{T}>(({T}*)a->scratch[{sc}], ({T}*)P.p[{out_slot}], "
+                        f"P.S, P.length, {L}, (cudaStream_t)stream)) return e;")
         else:
-            call = (f"return kun::launch_diffwsum<{T}>((const {T}*)P.p[{in_slots[0]}] + ({in_user[0]} ? P.start : 0) * P.S, "
-                    f"(const {T}*)P.p[{in_slots[1]}] + ({in_user[1]} ? P.start : 0) * P.S, "
-                    f"({T}*)P.p[{out_slot}], P.S, P.length, (cudaStream_t)stream);")
+            argout = f"({T}*)P.p[{out_slot}]"
+        if kind == "rank":
+            call = f"kun::launch_rank<{T}>({argin[0]}, {argout}, P.S, P.length, (cudaStream_t)stream)"
+        elif kind == "scale":
+            call = f"kun::launch_scale<{T}>({argin[0]}, {argout}, P.S, P.length, (cudaStream_t)stream)"
+        else:
+            call = f"kun::launch_diffwsum<{T}>({argin[0]}, {argin[1]}, {argout}, P.S, P.length, (cudaStream_t)stream)"
         fill = "\n".join(f"  P.p[{sl}] = a->buffers[{bid}];" for bid, sl in self.slots.items())
+        body = "\n".join(pre + [f"  if (int e = {call}) return e;"] + post + ["  return 0;"])
         launch = f"""
 extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
   {pstruct} P;
 {fill}
   P.S = a->num_stocks; P.total_time = a->total_time; P.start = a->start; P.length = a->length;
   if (a->num_stocks <= 0 || a->length <= 0) return 0;
-  {call}
+{body}
 }}
 """
         return src, launch

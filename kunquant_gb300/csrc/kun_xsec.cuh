@@ -541,6 +541,38 @@ __global__ void __launch_bounds__(256) diffwsum_segments(const T *__restrict__ i
     for (long long i = threadIdx.x; i < len; i += blockDim.x) orow[i] = ksub(a[i], sum);
 }
 
+// STs <-> TS row copies around the cross-sectional kernels: rows
+// [row0, row0 + length) of an [S/L][T_in][L] buffer to a [length][S] one, and
+// back to an [S/L][length][L] buffer.
+template <typename T>
+__global__ void sts_rows_to_ts(const T *__restrict__ in, T *__restrict__ out, long long S, long long T_in,
+                               long long row0, long long length, int L) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= length * S) return;
+    const long long t = i / S, s = i % S;
+    out[i] = in[(s / L) * T_in * L + (row0 + t) * L + s % L];
+}
+template <typename T>
+__global__ void ts_rows_to_sts(const T *__restrict__ in, T *__restrict__ out, long long S, long long length, int L) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= length * S) return;
+    const long long t = i / S, s = i % S;
+    out[(s / L) * length * L + t * L + s % L] = in[i];
+}
+template <typename T>
+inline int launch_sts_to_ts(const T *in, T *out, long long S, long long T_in, long long row0, long long length, int L,
+                            cudaStream_t st) {
+    const long long n = length * S;
+    sts_rows_to_ts<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, S, T_in, row0, length, L);
+    return (int)cudaGetLastError();
+}
+template <typename T>
+inline int launch_ts_to_sts(const T *in, T *out, long long S, long long length, int L, cudaStream_t st) {
+    const long long n = length * S;
+    ts_rows_to_sts<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(in, out, S, length, L);
+    return (int)cudaGetLastError();
+}
+
 inline int kun_num_sms() {
     static int n = 0;
     if (!n) {
