@@ -48,6 +48,22 @@ WORKLOADS = {
 }
 
 
+def max_over_ranks(ms: float, dist, device: str) -> float:
+    """The slowest rank's step time (the whole job ends with it)."""
+    if dist is None:
+        return ms
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_value(world: int, stocks: int, days: int, ms: float) -> float:
+    """Whole-job stock-days/s: every rank runs its own replica of the
+    workload (weak scaling), all done when the slowest one is."""
+    return world * stocks * days / (ms / 1e3)
+
+
 def _dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -349,11 +365,8 @@ def main():
         for sid, ms in ex.stage_times():
             stage_ms.setdefault(sid, []).append(ms)
     ex.set_profiling(False)
-    if dist:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
-    value = world * S * T / (ms_step / 1e3)
+    ms_step = max_over_ranks(ms_step, dist, "cuda")
+    value = job_value(world, S, T, ms_step)
 
     # dominant kernel and its HBM roofline
     avg = {sid: float(np.mean(v)) for sid, v in stage_ms.items()}

@@ -1,0 +1,55 @@
+"""The multi-replica path of bench.py on CPU ranks (gloo, world size 2):
+the step time is the slowest rank's, the value counts every rank's
+replica, and the reference arm prints from rank 0 only."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _rank_main(rank, world, port, q):
+    sys.path.insert(0, REPO)
+    import bench
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    ms = bench.max_over_ranks([3.0, 7.5][rank], dist, "cpu")
+    q.put((rank, ms, bench.job_value(world, 5000, 2500, ms)))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_max_over_ranks_and_value_gloo():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = 29500 + os.getpid() % 1000
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(60)
+        assert p.exitcode == 0
+    for _, ms, value in res:
+        assert ms == 7.5
+        assert value == pytest.approx(2 * 5000 * 2500 / 7.5e-3)
+
+
+def test_reference_arm_prints_from_rank0_only(tmp_path):
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    port = 30500 + os.getpid() % 1000
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--stocks", "200", "--days", "120"]
+    r = subprocess.run(cmd, cwd=REPO, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["cpu_baseline"]["kind"] == "port"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0
