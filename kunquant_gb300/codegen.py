@@ -525,7 +525,7 @@ def _c_str(s: str) -> str:
     return '"' + s.replace("\\", "\\\\").replace('"', '\\"') + '"'
 
 
-def generate_module(spec: dict, out_dir: str, tag: str = None, stages_per_file: int = 8,
+def generate_module(spec: dict, out_dir: str, tag: str = None, stages_per_file: int = 8, file_bytes: int = 48000,
                     mode: str = "leveled") -> List[str]:
     """Write the CUDA sources of one module; returns the list of .cu paths."""
     os.makedirs(out_dir, exist_ok=True)
@@ -577,7 +577,9 @@ template <> struct LogTables<{T}> {{
         if g.kernel_info:
             kinfo[si] = g.kernel_info
         cur.append(src)
-        if len(cur) >= stages_per_file:
+        # translation units of similar size compile in parallel in about
+        # the time of the largest one
+        if len(cur) >= stages_per_file or sum(len(c) for c in cur) >= file_bytes:
             files.append(cur)
             cur = []
     if cur:

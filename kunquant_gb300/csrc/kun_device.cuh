@@ -38,6 +38,13 @@ template <typename T> __device__ __forceinline__ T knan() {
 template <typename T> __device__ __forceinline__ T kinf() {
     return kfrom((typename FpBits<T>::U)(sizeof(T) == 4 ? 0x7f800000ull : 0x7ff0000000000000ull), T());
 }
+// read of row `row` of a [T][S] series column (stride st): NaN outside
+// [0, length) when EDGE; interior tiles, whose rows are all inside, skip the test
+template <bool EDGE, typename T>
+__device__ __forceinline__ T ldw(const T* __restrict__ p, long long st, long long row, long long length) {
+    if (EDGE) return (unsigned long long)row < (unsigned long long)length ? p[row * st] : knan<T>();
+    return p[row * st];
+}
 // boolean results are all-ones / all-zeros bit masks, as SIMD compares produce
 template <typename T> __device__ __forceinline__ T kmask(bool b) {
     using U = typename FpBits<T>::U;

@@ -18,6 +18,7 @@ cheap pointwise ops are recomputed where they are needed.  A windowed read
 earlier level, so every kernel reads exactly the values the sequential
 reference computes and the arithmetic of every op is unchanged.
 """
+import os
 from typing import Dict, List, Optional, Set, Tuple
 
 from . import contraction
@@ -454,6 +455,9 @@ from .codegen import StageGen  # noqa: E402
 PAR_CHUNK = 32
 REG_WINDOW_MAX = 64
 VEC_U = 4
+# rows a window queue loads ahead of use, and the unroll of the window loop
+VEC_PREFETCH = int(os.environ.get("KUN_VEC_PREFETCH", "0"))
+VEC_UNROLL = int(os.environ.get("KUN_VEC_UNROLL", "2"))
 SCAN_BLOCK = 16
 WIDE_SERIES = 24
 
@@ -818,12 +822,15 @@ class LeveledGen(StageGen):
 
     # ------------------------------------------------------------------ vector form
     def _vload(self, j: int, texpr: str) -> str:
-        """Guarded read of series j at row `texpr` (NaN outside [0, length))."""
-        return (f"(((long long)({texpr}) >= 0 && (long long)({texpr}) < length) ? "
-                f"b{j}[(long long)({texpr}) * st{j}] : kun::knan<{self.T}>())")
+        """Read of series j at row `texpr`, NaN outside [0, length); the test
+        is compiled out of the interior instance of the body (KE false)."""
+        self.edge_body = True
+        return f"kun::ldw<KE>(b{j}, st{j}, (long long)({texpr}), length)"
 
     def _emit_par_vec(self, comp: Set[int], vr: Set[int], stores: List[int], loops, U: int, ind: str):
         ops, T = self.ops, self.T
+        # a window queue holds the U rows in use and VEC_PREFETCH rows ahead
+        QL = U + VEC_PREFETCH
         self.cur_comp = comp
         self.vec = True
         L = self.lines
@@ -873,10 +880,10 @@ class LeveledGen(StageGen):
                         qn = f"q{head}_{src}"
                         queues[key] = qn
                         wh = ops[head]["window"]
-                        L.append(f"{ind}{T} {qn}[{U}];")
+                        L.append(f"{ind}{T} {qn}[{QL}];")
                         L.append(f"{ind}#pragma unroll")
-                        L.append(f"{ind}for (int u = 0; u < {U}; ++u) {qn}[u] = {self._vload(src, f't + u - {wh - 1}')};")
-                L.append(f"{ind}#pragma unroll 2")
+                        L.append(f"{ind}for (int u = 0; u < {QL}; ++u) {qn}[u] = {self._vload(src, f't + u - {wh - 1}')};")
+                L.append(f"{ind}#pragma unroll {VEC_UNROLL}")
                 L.append(f"{ind}for (int iter = {w - 1}; iter >= {seg}; --iter) {{")
                 bi = ind + "  "
                 L.append(f"{bi}#pragma unroll")
@@ -899,8 +906,8 @@ class LeveledGen(StageGen):
                 for src in srcs:
                     qn = queues[(head, src)]
                     L.append(f"{bi}#pragma unroll")
-                    L.append(f"{bi}for (int u = 0; u < {U - 1}; ++u) {qn}[u] = {qn}[u + 1];")
-                    L.append(f"{bi}{qn}[{U - 1}] = {self._vload(src, f't + {U} - iter')};")
+                    L.append(f"{bi}for (int u = 0; u < {QL - 1}; ++u) {qn}[u] = {qn}[u + 1];")
+                    L.append(f"{bi}{qn}[{QL - 1}] = {self._vload(src, f't + {QL} - iter')};")
                 L.append(f"{ind}}}")
             elif k in REDUCTIONS:
                 pass
@@ -972,6 +979,7 @@ class LeveledGen(StageGen):
             seen: Set[int] = set()
             self.lines = []
             self.cur_level = L
+            self.edge_body = False
             if kd["kind"] == "par":
                 comp, vr, wr = kd["comp"], kd["vr"], kd["wr"]
                 for j in sorted(vr | wr | {i for i in comp if ops[i]["k"] in ("Output", "WindowedTempOutput")}
@@ -1038,9 +1046,23 @@ class LeveledGen(StageGen):
                 self.lines.append("  }")
                 kinfo.append((len(roles), 1))
             # the body takes its block coordinates as arguments, so the same
-            # code serves a launch of one job and a grouped launch of many
+            # code serves a launch of one job and a grouped launch of many.
+            # A vector-form body comes in two instances: KE (edge) tests every
+            # row it reads against [0, length); the interior one serves tiles
+            # whose reads, rows [t0 - wmax, t1 + fwd), all lie inside.
+            if self.edge_body:
+                wmax = max([int(o[k]) for o in ops for k in ("window", "loop_window")
+                            if isinstance(o.get(k), int)] + [0]) + VEC_U
+                fwd = VEC_U + VEC_PREFETCH
+                tmpl = "template <bool KE> "
+                pick = (f"  const long long t0_ = (long long)by * P.tile[{ki}];\n"
+                        f"  const long long t1_ = t0_ + P.tile[{ki}] < P.length ? t0_ + P.tile[{ki}] : P.length;\n"
+                        f"  if (t0_ >= {wmax} && t1_ + {fwd} <= P.length) {kname}_body<false>(P, bx, by);\n"
+                        f"  else {kname}_body<true>(P, bx, by);")
+            else:
+                tmpl, pick = "", f"  {kname}_body(P, bx, by);"
             srcs.append(f"""
-__device__ __forceinline__ void {kname}_body(const {pstruct}& P, const int bx, const int by) {{
+{tmpl}__device__ __forceinline__ void {kname}_body(const {pstruct}& P, const int bx, const int by) {{
   const long long S = P.S;
   const long long s = (long long)bx * blockDim.x + threadIdx.x;
   if (s >= S) return;
@@ -1050,14 +1072,16 @@ __device__ __forceinline__ void {kname}_body(const {pstruct}& P, const int bx, c
 {chr(10).join(self.lines)}
 }}
 __global__ void __launch_bounds__(KUN_TS_THREADS) {kname}(const {pstruct} P) {{
-  {kname}_body(P, blockIdx.x, blockIdx.y);
+  const int bx = blockIdx.x, by = blockIdx.y;
+{pick}
 }}
 __global__ void __launch_bounds__(KUN_TS_THREADS) {kname}_grp(const {pstruct}* __restrict__ jobs, const kun::TileTable tt) {{
   const int j = kun::tile_job(tt, blockIdx.x);
   const {pstruct}& P = jobs[j];
   const int local = (int)blockIdx.x - tt.off[j];
   const int gx = (int)((P.S + blockDim.x - 1) / blockDim.x);
-  {kname}_body(P, local % gx, local / gx);
+  const int bx = local % gx, by = local / gx;
+{pick}
 }}
 """)
         nslots = max(1, len(self.slots))
