@@ -18,7 +18,6 @@ cheap pointwise ops are recomputed where they are needed.  A windowed read
 earlier level, so every kernel reads exactly the values the sequential
 reference computes and the arithmetic of every op is unchanged.
 """
-import os
 from typing import Dict, List, Optional, Set, Tuple
 
 from . import contraction
@@ -456,8 +455,8 @@ PAR_CHUNK = 32
 REG_WINDOW_MAX = 64
 VEC_U = 4
 # rows a window queue loads ahead of use, and the unroll of the window loop
-VEC_PREFETCH = int(os.environ.get("KUN_VEC_PREFETCH", "0"))
-VEC_UNROLL = int(os.environ.get("KUN_VEC_UNROLL", "2"))
+VEC_PREFETCH = 0
+VEC_UNROLL = 4
 SCAN_BLOCK = 16
 WIDE_SERIES = 24
 
