@@ -161,12 +161,16 @@ def cpu_reference(workload: dict, steps: int, warmup: int, seconds_target: float
             "s_per_step": dt}
 
 
-def serving(nsess=256, steps=30, seed=3):
+def serving(nsess=256, rate=20000.0, seconds=3.0, warm=250, seed=3):
     """Stream serving of the Alpha101 stream module: `nsess` sessions of
-    log-uniform size in [100, 5000] stocks in one pool; every step all
-    sessions submit one tick through the request loop and wait for it.
-    Returns the per-tick latency (submit to result in the pinned host table)
-    percentiles and the throughput."""
+    log-uniform size in [100, 5000] stocks in one pool, each warmed with
+    `warm` days of history.  Bars then arrive as a Poisson process at an
+    aggregate `rate` session-ticks/s (each to a session drawn uniformly);
+    a session with a tick in flight queues its next bar.  The request loop
+    batches whatever is submitted while a step runs.  Latency is arrival to
+    result in the pinned host table.  For contrast, the same ticks through one
+    StreamContext per session, called one after another."""
+    from collections import deque
     from kunquant_gb300 import runner as kr
     from kunquant_gb300 import serve
     mod = kr.Library.predefined("alpha101_stream_f32").getModule("alpha101_stream")
@@ -178,26 +182,81 @@ def serving(nsess=256, steps=30, seed=3):
     sess = [pool.open(int(n)) for n in sizes]
     names = mod.getInputNames()
     base = rng.uniform(10, 100, cap).astype(np.float32)
-    warm = 10
-    for st in range(steps + warm):
-        for s in sess:
-            row = base[s.column:s.column + s.num_stocks] * np.float32(1 + 0.001 * st)
-            for k in names:
-                s.inputs[k][:] = row
+    day = [0] * nsess
+
+    def write(i):
+        s = sess[i]
+        row = base[s.column:s.column + s.num_stocks] * np.float32(1 + 0.001 * (day[i] % 100))
+        for k in names:
+            s.inputs[k][:] = row
+        day[i] += 1
+
+    # history: every session steps through `warm` days together
+    for _ in range(warm):
+        for i in range(nsess):
+            write(i)
         pool.submit_all(sess)
         for s in sess:
             s.wait(60000)
-        if st == warm - 1:
-            pool.take_latencies()
-            t0 = time.perf_counter()
+    pool.take_latencies()
+    # Poisson arrivals
+    n_arr = int(rate * seconds)
+    arr_t = np.cumsum(rng.exponential(1.0 / rate, n_arr))
+    arr_s = rng.integers(0, nsess, n_arr)
+    pending = [deque() for _ in range(nsess)]
+    inflight, waiting = {}, set()
+    lat = []
+    i = 0
+    t0 = time.perf_counter()
+    while i < n_arr or inflight or waiting:
+        now = time.perf_counter() - t0
+        while i < n_arr and arr_t[i] <= now:
+            j = int(arr_s[i])
+            pending[j].append(arr_t[i])
+            if j not in inflight:
+                waiting.add(j)
+            i += 1
+        done = [j for j in inflight if sess[j].ticks >= sess[j]._submitted]
+        if done:
+            tdone = time.perf_counter() - t0
+            for j in done:
+                lat.append(tdone - inflight.pop(j))
+                if pending[j]:
+                    waiting.add(j)
+        if waiting:
+            batch = list(waiting)
+            waiting.clear()
+            for j in batch:
+                write(j)
+                inflight[j] = pending[j].popleft()
+            pool.submit_all([sess[j] for j in batch])
     el = time.perf_counter() - t0
-    lat, sz = pool.take_latencies()
+    _, steps = pool.take_latencies()
     pool.shutdown()
-    return {"module": "alpha101_stream_f32", "sessions": nsess, "stocks": cap, "steps": steps,
-            "sizes": "log-uniform [100, 5000] stocks per session",
-            "p50_tick_us": float(np.percentile(lat, 50)), "p99_tick_us": float(np.percentile(lat, 99)),
-            "stock_ticks_per_s": cap * steps / el, "ms_per_step": el / steps * 1e3,
-            "pool_bytes": serve.pool_bytes(mod, cap)}
+    lat = np.asarray(lat) * 1e6
+    # the same kind of tick through one StreamContext per session, one call after another
+    k = min(32, nsess)
+    ctxs = [kr.StreamContext(ex, mod, int(sizes[j])) for j in range(k)]
+    hs = [{n: c.queryBufferHandle(n) for n in names} for c in ctxs]
+    rows = [base[:int(sizes[j])] for j in range(k)]
+    for rep in range(3):
+        if rep == 1:
+            tp = time.perf_counter()
+        for c, h, r in zip(ctxs, hs, rows):
+            for n in names:
+                c.pushData(h[n], r)
+            c.run()
+    per_call = (time.perf_counter() - tp) / (2 * k)
+    return {"module": "alpha101_stream_f32", "sessions": nsess, "stocks": cap,
+            "sizes": "log-uniform [100, 5000] stocks per session", "history_days": warm,
+            "arrivals": f"Poisson, {rate:.0f} session-ticks/s aggregate, {seconds:.0f} s",
+            "ticks": int(lat.size), "p50_tick_us": float(np.percentile(lat, 50)),
+            "p99_tick_us": float(np.percentile(lat, 99)), "session_ticks_per_s": lat.size / el,
+            "stock_ticks_per_s": float(lat.size / el * sizes.mean()),
+            "mean_sessions_per_step": float(np.mean(steps)) if len(steps) else None,
+            "pool_bytes": serve.pool_bytes(mod, cap),
+            "one_context_per_session": {"ms_per_session_tick": per_call * 1e3,
+                                        "max_session_ticks_per_s": 1.0 / per_call}}
 
 
 def universes_main(args):
@@ -256,6 +315,94 @@ def universes_main(args):
     print(json.dumps(line))
 
 
+PRECISION_FORMS = {
+    "alpha158": ["alpha158_f32", "alpha158_fast_f32", "alpha158_comp_f32", "alpha158_acc64_f32"],
+    "alpha101": ["alpha101_f32", "alpha101_comp_f32", "alpha101_acc64_f32"],
+}
+
+
+def _factor_errors(got, want):
+    """Per factor (max rel err, median rel err, NaN cells that differ) of a
+    fp32 form against the fp64 build, on the GPU.  The relative error is
+    |got - want| / max(|want|, 1e-3 * median |want|) over cells where both
+    are numbers (the floor keeps values crossing zero from dividing by ~0)."""
+    import torch
+    out = {}
+    for k, w in want.items():
+        g = got[k].double()
+        gn, wn = torch.isnan(g), torch.isnan(w)
+        nanmis = int((gn != wn).sum())
+        both = ~gn & ~wn
+        if bool(both.any()):
+            wb, gb = w[both], g[both]
+            m = wb.abs().median()
+            rel = (gb - wb).abs() / torch.clamp(wb.abs(), min=float(1e-3 * m + 1e-30))
+            out[k] = (float(rel.max()), float(rel.median()), nanmis)
+        else:
+            out[k] = (0.0, 0.0, nanmis)
+    return out
+
+
+def precision_main(args):
+    """Per-factor error of the fp32 forms (exact fp32, fast-stat, two-float
+    compensated sums, fp64 sums) against the fp64 build, on Alpha158 and
+    Alpha101 over S x T cells of seeded OHLCV whose price levels are drawn
+    log-uniform in [1, 1e5].  The fp64 build is the truth: it reproduces the
+    reference's fp64 TS build bit for bit (the fp64 parity tests)."""
+    import torch
+    from kunquant_gb300 import runner as kr
+    from kunquant_gb300 import synth
+    torch.cuda.set_device(0)
+    S, T = args.stocks or 8192, args.days or 4000
+    d32 = synth.ohlcv(S, T, seed=77, nan_frac=0.0, price_range=(1.0, 1e5))
+    in32 = {k: torch.from_numpy(v).cuda() for k, v in d32.items()}
+    in64 = {k: v.double() for k, v in in32.items()}
+    ex = kr.createSingleThreadExecutor()
+    summary, tables = {}, []
+    for graph, forms in PRECISION_FORMS.items():
+        m64 = kr.Library.predefined(f"{graph}_f64").getModule(graph)
+        want = kr.runGraph(ex, m64, in64, 0, T)
+        stats = {}
+        for key in forms:
+            name = key[:-4]
+            mod = kr.Library.predefined(key).getModule(name)
+            got = kr.runGraph(ex, mod, in32, 0, T)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            kr.runGraph(ex, mod, in32, 0, T, outputs=got)
+            e1.record()
+            torch.cuda.synchronize()
+            st = stats[name] = _factor_errors(got, want)
+            del got
+            med = [v[1] for v in st.values()]
+            summary[name] = {"factors": len(st), "max_le_1e-5": sum(v[0] <= 1e-5 for v in st.values()),
+                             "median_le_1e-5": sum(m <= 1e-5 for m in med),
+                             "worst_median": max(med), "nan_cells_differing": sum(v[2] for v in st.values()),
+                             "ms": e0.elapsed_time(e1)}
+        del want
+        torch.cuda.empty_cache()
+        names = sorted(next(iter(stats.values())))
+        tables.append(f"## {graph}\n\n| factor | " + " | ".join(f"{n} max | {n} median | {n} NaN diff" for n in stats)
+                      + " |\n|---|" + "---|---|---|" * len(stats))
+        for f in names:
+            tables.append(f"| {f} | " + " | ".join(f"{stats[n][f][0]:.1e} | {stats[n][f][1]:.1e} | {stats[n][f][2]}"
+                                                  for n in stats) + " |")
+        tables.append("")
+    if args.report:
+        with open(args.report, "w") as f:
+            f.write(f"# fp32 forms vs the fp64 build, {S} stocks x {T} days, prices log-uniform in [1, 1e5]\n\n")
+            for n, v in summary.items():
+                f.write(f"- {n}: {json.dumps(v)}\n")
+            f.write("\n" + "\n".join(tables))
+    line = {"metric": "factors with median rel err <= 1e-5", "value": summary["alpha158_comp"]["median_le_1e-5"],
+            "unit": "factors", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"precision: alpha158 + alpha101, {S} stocks x {T} days, price levels "
+                                   f"log-uniform in [1, 1e5], truth = the fp64 build"},
+            "forms": summary}
+    print(json.dumps(line))
+
+
 def stage_bytes(mod_spec, stage_idx, S, T, elem):
     st = mod_spec["stages"][stage_idx]
     return (len(set(st["in"])) + len(st["out"])) * S * T * elem
@@ -267,7 +414,8 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="alpha158", choices=sorted(WORKLOADS) + ["universes"])
+    ap.add_argument("--workload", default="alpha158", choices=sorted(WORKLOADS) + ["universes", "precision"])
+    ap.add_argument("--report", default=None, help="precision workload: write the per-factor table here")
     ap.add_argument("--stocks", type=int, default=None)
     ap.add_argument("--days", type=int, default=None)
     ap.add_argument("--no-e2e", action="store_true")
@@ -277,6 +425,12 @@ def main():
     ap.add_argument("--universes", type=int, default=48, help="universes of the 'universes' workload")
     ap.add_argument("--streams", type=int, default=8, help="CUDA streams for concurrent stages")
     args = ap.parse_args()
+    if args.workload == "precision":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the precision workload compares the GPU forms "
+                              "with each other; the reference arm times the batch workloads"}))
+            return
+        return precision_main(args)
     if args.workload == "universes":
         if args.impl == "reference":
             args.workload = "alpha158"  # the CPU arm times the same graph per stock-day

@@ -167,14 +167,17 @@ KunStatus kunRunGraphBatch(KunExecutorHandle exec, KunModuleHandle m, int njobs,
                            const size_t *total_time, const size_t *cur_time, const size_t *length,
                            int synchronize);
 /* Autotuner (GPU extension): time candidate launch shapes (time tile x
- * threads per block) of every time-series stage on these jobs and keep the
- * fastest per stage; the executor then uses them for this module in
+ * threads per block, and per time-parallel kernel its instance compiled for
+ * 64 registers a thread) of every time-series stage on these jobs and keep
+ * the fastest per stage; the executor then uses them for this module in
  * kunRunGraphBatch and kunRunGraphEx.  Computes the jobs' outputs on the way.
  * Returns the number of stages tuned, -1 on error. */
 int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle m, int njobs, const KunBufferNameMapHandle *buffers,
                     const size_t *num_stocks, const size_t *total_time, const size_t *cur_time,
                     const size_t *length, int reps);
-/* Tuned shape of one stage (kernel count, 0 if untuned) and clearing it. */
+/* Tuned shape of one stage (kernel count, 0 if untuned) and clearing it.
+ * A block entry or'd with KUN_BLOCK_REGCAP names the 64-register instance. */
+#define KUN_BLOCK_REGCAP 0x10000
 int kunExecutorTunedShape(KunExecutorHandle exec, KunModuleHandle m, int stage, int32_t *tile, int32_t *block,
                           int cap);
 KunStatus kunExecutorClearTuning(KunExecutorHandle exec);

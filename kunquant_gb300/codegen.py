@@ -541,6 +541,9 @@ def generate_module(spec: dict, out_dir: str, tag: str = None, stages_per_file: 
 #ifndef KUN_TS_THREADS
 #define KUN_TS_THREADS 128
 #endif
+#ifndef KUN_TS_MINB
+#define KUN_TS_MINB 1
+#endif
 namespace kun {{
 template <> struct LogTables<{T}> {{
   static __device__ __forceinline__ {T} r(unsigned long long i) {{

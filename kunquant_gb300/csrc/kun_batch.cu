@@ -273,10 +273,12 @@ KUN_EXPORT KunStatus kunRunGraphBatch(KunExecutorHandle exec, KunModuleHandle mo
 
 // Tune the launch shapes of every grouped-capable stage on these jobs (the
 // jobs' outputs are computed along the way).  Candidates: time tiles
-// {default, 16, 32, 64, 128, 256} x {64, 128} threads per block for the
-// time-parallel kernels; {32, 64, 128} threads for the scan kernels.  Each
-// candidate runs the stage `reps` times after one warm-up; the fastest mean
-// wins.  Returns the number of stages tuned, or -1 on error.
+// {default, 16, 32, 64, 128, 256} x {64, 128} threads per block for all the
+// time-parallel kernels of a stage together, {32, 64, 128} threads for its
+// scan kernels; then per time-parallel kernel, with the others held: its
+// 64-register instance or not x block size, then its tile.  Each candidate
+// runs the stage `reps` times after one warm-up; the fastest mean wins.
+// Returns the number of stages tuned, or -1 on error.
 KUN_EXPORT int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle mod, int njobs,
                                const KunBufferNameMapHandle *buffers, const size_t *num_stocks,
                                const size_t *total_time, const size_t *cur_time, const size_t *length, int reps) {
@@ -316,12 +318,8 @@ KUN_EXPORT int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle mod, int 
         for (int k = 0; k < nk; k++) (d.kernel_info[k] & 1 ? has_scan : has_par) = true;
         std::vector<int32_t> best_t(nk, 0), best_b(nk, 0), t(nk), b(nk);
         float best = -1.f;
-        auto trial = [&](int tile, int blk, int sblk) -> bool {
-            for (int k = 0; k < nk; k++) {
-                const bool scan = d.kernel_info[k] & 1;
-                t[k] = scan ? 0 : tile;
-                b[k] = scan ? sblk : blk;
-            }
+        // times the stage with shape (t, b); keeps it when fastest so far
+        auto run = [&]() -> bool {
             br.host_off = 0;  // earlier trials of this stage are complete below
             if (batch_stage(br, si, st, t.data(), b.data(), launches) != KUN_SUCCESS) return false;
             cudaEventRecord(e0, st);
@@ -339,6 +337,15 @@ KUN_EXPORT int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle mod, int 
             }
             return true;
         };
+        auto trial = [&](int tile, int blk, int sblk) -> bool {
+            for (int k = 0; k < nk; k++) {
+                const bool scan = d.kernel_info[k] & 1;
+                t[k] = scan ? 0 : tile;
+                b[k] = scan ? sblk : blk;
+            }
+            return run();
+        };
+        // one shape for every kernel of the stage first
         for (int tile : tiles) {
             if (!has_par && tile != 0) continue;
             for (int blk : blocks) {
@@ -356,6 +363,28 @@ KUN_EXPORT int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle mod, int 
                         blk = pb[k];
                     }
                 if (!trial(tile, blk, sblk)) return -1;
+            }
+        }
+        // then each time-parallel kernel on its own: the 64-register
+        // instance and the block size, then the tile, the others held at
+        // their best
+        for (int k = 0; k < nk && has_par; k++) {
+            if (d.kernel_info[k] & 1) continue;
+            for (int cap : {0, (int)KUN_BLOCK_REGCAP}) {
+                for (int blk : blocks) {
+                    t = best_t;
+                    b = best_b;
+                    b[k] = blk | cap;
+                    if (b[k] == best_b[k]) continue;
+                    if (!run()) return -1;
+                }
+            }
+            for (int tile : tiles) {
+                t = best_t;
+                b = best_b;
+                if (tile == t[k]) continue;
+                t[k] = tile;
+                if (!run()) return -1;
             }
         }
         table[si].tile = best_t;

@@ -11,7 +11,8 @@
 extern "C" {
 #endif
 
-#define KUN_GPU_MODULE_ABI 0x6b470006ull
+#define KUN_GPU_MODULE_ABI 0x6b470007ull
+#define KUN_BLOCK_REGCAP 0x10000
 
 typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
 typedef enum { KUN_BUF_INPUT = 0, KUN_BUF_OUTPUT = 1, KUN_BUF_TEMP = 2 } KunGpuBufferKind;
@@ -59,7 +60,8 @@ typedef struct {
     const int32_t *seg_count;
     /* optional per-kernel launch shape of a time-series stage (num_kernels
      * entries, 0 = default): time tile in rows (a multiple of 4) and threads
-     * per block (at most 128) */
+     * per block (at most 128), or'd with KUN_BLOCK_REGCAP to launch the
+     * time-parallel kernel's instance compiled for 64 registers a thread */
     const int32_t *tune_tile;
     const int32_t *tune_block;
 } KunGpuStageArgs;

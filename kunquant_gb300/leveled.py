@@ -454,6 +454,9 @@ from .codegen import StageGen  # noqa: E402
 PAR_CHUNK = 32
 REG_WINDOW_MAX = 64
 VEC_U = 4
+# rows a thread computes at once in a kernel without window loops, where
+# the rows share no loads and more of them only cost registers
+VEC_U_ELEM = 2
 # rows a window queue loads ahead of use, and the unroll of the window loop
 VEC_PREFETCH = 0
 VEC_UNROLL = 4
@@ -1012,12 +1015,14 @@ class LeveledGen(StageGen):
                 # wide kernels (many series in and out) keep one row per
                 # iteration: the 4-row form would not fit in registers
                 wide = len(vr) + len(stores) + sum(1 for i in comp if ops[i]["k"] == "Output") > WIDE_SERIES
-                if sls or VEC_U <= 1 or wide:
+                U = VEC_U if any(ops[i]["k"] == "ForeachBackWindow" for i in comp) else VEC_U_ELEM
+                if sls or U <= 1 or wide:
                     self.lines.append("  for (long long t = t0; t < t1; ++t) {")
                     self._body(comp, vr, stores, loops, "    ")
                 else:
-                    self.lines.append(f"  for (long long t = t0; t < t1; t += {VEC_U}) {{")
-                    self._emit_par_vec(comp, vr, stores, loops, VEC_U, "    ")
+                    self.lines.append(f"  for (long long t = t0; t < t1; t += {U}) {{")
+                    self._emit_par_vec(comp, vr, stores, loops, U, "    ")
+                    self.vec_u = U
                 self.lines.append("  }")
                 kinfo.append((chunk, 0))
             else:
@@ -1051,8 +1056,8 @@ class LeveledGen(StageGen):
             # whose reads, rows [t0 - wmax, t1 + fwd), all lie inside.
             if self.edge_body:
                 wmax = max([int(o[k]) for o in ops for k in ("window", "loop_window")
-                            if isinstance(o.get(k), int)] + [0]) + VEC_U
-                fwd = VEC_U + VEC_PREFETCH
+                            if isinstance(o.get(k), int)] + [0]) + self.vec_u
+                fwd = self.vec_u + VEC_PREFETCH
                 tmpl = "template <bool KE> "
                 pick = (f"  const long long t0_ = (long long)by * P.tile[{ki}];\n"
                         f"  const long long t1_ = t0_ + P.tile[{ki}] < P.length ? t0_ + P.tile[{ki}] : P.length;\n"
@@ -1070,11 +1075,16 @@ class LeveledGen(StageGen):
 {chr(10).join(decl)}
 {chr(10).join(self.lines)}
 }}
-__global__ void __launch_bounds__(KUN_TS_THREADS) {kname}(const {pstruct} P) {{
+""")
+            # time-parallel kernels also come compiled for 64 registers a
+            # thread (8 blocks of 128 threads an SM), picked per kernel by the
+            # tuner; scan kernels keep one instance
+            for suf, minb in ([("", "KUN_TS_MINB"), ("_r", "8")] if kd["kind"] == "par" else [("", "KUN_TS_MINB")]):
+                srcs.append(f"""__global__ void __launch_bounds__(KUN_TS_THREADS, {minb}) {kname}{suf}(const {pstruct} P) {{
   const int bx = blockIdx.x, by = blockIdx.y;
 {pick}
 }}
-__global__ void __launch_bounds__(KUN_TS_THREADS) {kname}_grp(const {pstruct}* __restrict__ jobs, const kun::TileTable tt) {{
+__global__ void __launch_bounds__(KUN_TS_THREADS, {minb}) {kname}{suf}_grp(const {pstruct}* __restrict__ jobs, const kun::TileTable tt) {{
   const int j = kun::tile_job(tt, blockIdx.x);
   const {pstruct}& P = jobs[j];
   const int local = (int)blockIdx.x - tt.off[j];
@@ -1100,16 +1110,21 @@ struct {pstruct} {{
         # arrays when given
         sel = []
         for k, (d, sc) in enumerate(kinfo):
-            sel.append(f"  const int blk{k} = (a->tune_block && a->tune_block[{k}] > 0) ? a->tune_block[{k}] : KUN_TS_THREADS;")
+            sel.append(f"  const int tb{k} = (a->tune_block && a->tune_block[{k}] > 0) ? a->tune_block[{k}] : KUN_TS_THREADS;")
+            sel.append(f"  const int blk{k} = tb{k} & 0xffff;")
             if not sc:
                 sel.append(f"  P.tile[{k}] = (a->tune_tile && a->tune_tile[{k}] > 0) ? a->tune_tile[{k}] : {d};")
             else:
                 sel.append(f"  P.tile[{k}] = 0;")
         for k, (d, sc) in enumerate(kinfo):
             gy = str(d) if sc else f"(unsigned)((a->length + P.tile[{k}] - 1) / P.tile[{k}])"
-            calls.append(f"  {knames[k]}<<<dim3((unsigned)((a->num_stocks + blk{k} - 1) / blk{k}), {gy}), blk{k}, 0, "
-                         f"(cudaStream_t)stream>>>(P);\n"
-                         f"  if (cudaError_t e = cudaGetLastError()) return (int)e;")
+            grid = f"dim3((unsigned)((a->num_stocks + blk{k} - 1) / blk{k}), {gy}), blk{k}, 0, (cudaStream_t)stream"
+            if sc:
+                calls.append(f"  {knames[k]}<<<{grid}>>>(P);")
+            else:
+                calls.append(f"  if (tb{k} & KUN_BLOCK_REGCAP) {knames[k]}_r<<<{grid}>>>(P);\n"
+                             f"  else {knames[k]}<<<{grid}>>>(P);")
+            calls.append("  if (cudaError_t e = cudaGetLastError()) return (int)e;")
         launch = self.launcher(pstruct, "\n".join(sel + calls))
         launch += self._group_launcher(pstruct, knames, kinfo)
         return head + "".join(srcs), launch
@@ -1129,8 +1144,14 @@ struct {pstruct} {{
         for k, (d, sc) in enumerate(kinfo):
             gy = str(d) if sc else f"(a->length + tile - 1) / tile"
             tl = "0" if sc else f"(a->tune_tile && a->tune_tile[{k}] > 0) ? a->tune_tile[{k}] : {d}"
+            kcall = (f"{knames[k]}_grp<<<(unsigned)total, blk, 0, (cudaStream_t)stream>>>((const {pstruct}*)dev, tt);"
+                     if sc else
+                     f"if (tb & KUN_BLOCK_REGCAP) {knames[k]}_r_grp<<<(unsigned)total, blk, 0, (cudaStream_t)stream>>>"
+                     f"((const {pstruct}*)dev, tt);\n      else {knames[k]}_grp<<<(unsigned)total, blk, 0, "
+                     f"(cudaStream_t)stream>>>((const {pstruct}*)dev, tt);")
             launches.append(f"""  {{
-    const int blk = (args[0].tune_block && args[0].tune_block[{k}] > 0) ? args[0].tune_block[{k}] : KUN_TS_THREADS;
+    const int tb = (args[0].tune_block && args[0].tune_block[{k}] > 0) ? args[0].tune_block[{k}] : KUN_TS_THREADS;
+    const int blk = tb & 0xffff;
     kun::TileTable tt;
     tt.njobs = njobs;
     long long total = 0;
@@ -1144,7 +1165,7 @@ struct {pstruct} {{
     tt.off[njobs] = (int)total;
     if (total > 0x7fffffffLL) return (int)cudaErrorInvalidValue;
     if (total > 0) {{
-      {knames[k]}_grp<<<(unsigned)total, blk, 0, (cudaStream_t)stream>>>((const {pstruct}*)dev, tt);
+      {kcall}
       if (cudaError_t e = cudaGetLastError()) return (int)e;
     }}
   }}""")

@@ -53,3 +53,28 @@ def test_reference_arm_prints_from_rank0_only(tmp_path):
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["cpu_baseline"]["kind"] == "port"
     assert d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_factor_errors_matches_numpy():
+    """The GPU precision report's error measure, run on CPU tensors, equals
+    the numpy form of the same definition."""
+    import numpy as np
+    import torch
+    sys.path.insert(0, REPO)
+    import bench
+    rng = np.random.default_rng(5)
+    w = rng.normal(size=(50, 40)) * 10
+    g = w * (1 + rng.normal(size=w.shape) * 1e-6)
+    w[3, 4] = np.nan
+    g[7, 1] = np.nan
+    w[9, 9] = 1e-9  # near zero: the floor applies
+    got = bench._factor_errors({"f": torch.from_numpy(g.astype(np.float32))}, {"f": torch.from_numpy(w)})["f"]
+    g32 = g.astype(np.float32).astype(np.float64)
+    both = ~np.isnan(w) & ~np.isnan(g32)
+    # torch's median of an even count is the lower middle value
+    a = np.sort(np.abs(w[both]))
+    m = a[(a.size - 1) // 2]
+    rel = np.abs(g32[both] - w[both]) / np.maximum(np.abs(w[both]), 1e-3 * m + 1e-30)
+    assert got[2] == 2
+    assert got[0] == pytest.approx(rel.max(), rel=1e-12)
+    assert got[1] == pytest.approx(np.sort(rel)[(rel.size - 1) // 2], rel=1e-12)
