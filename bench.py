@@ -40,6 +40,9 @@ WORKLOADS = {
     # fp32 factor arithmetic with two-float compensated fp32 running sums
     "alpha158_comp": dict(key="alpha158_comp_f32", module="alpha158_comp", stocks=5000, days=2500, nan=0.005,
                           n_inputs=6, n_outputs=158),
+    # Kahan fp32 window loops, two-float compensated rolling sums
+    "alpha158_mixed": dict(key="alpha158_mixed_f32", module="alpha158_mixed", stocks=5000, days=2500, nan=0.005,
+                           n_inputs=6, n_outputs=158),
     # the baseline form: one kernel launch per op, every value through HBM
     "alpha158_plain": dict(key="alpha158_plain_f32", module="alpha158_plain", stocks=5000, days=2500, nan=0.005,
                            n_inputs=6, n_outputs=158),
@@ -316,8 +319,9 @@ def universes_main(args):
 
 
 PRECISION_FORMS = {
-    "alpha158": ["alpha158_f32", "alpha158_fast_f32", "alpha158_comp_f32", "alpha158_acc64_f32"],
-    "alpha101": ["alpha101_f32", "alpha101_comp_f32", "alpha101_acc64_f32"],
+    "alpha158": ["alpha158_f32", "alpha158_fast_f32", "alpha158_mixed_f32", "alpha158_comp_f32",
+                 "alpha158_acc64_f32"],
+    "alpha101": ["alpha101_f32", "alpha101_mixed_f32", "alpha101_comp_f32", "alpha101_acc64_f32"],
 }
 
 
@@ -360,7 +364,7 @@ def precision_main(args):
     ex = kr.createSingleThreadExecutor()
     summary, tables = {}, []
     for graph, forms in PRECISION_FORMS.items():
-        m64 = kr.Library.predefined(f"{graph}_f64").getModule(graph)
+        m64 = kr.Library.predefined(f"{graph}_f64").getModule(f"{graph}_f64")
         want = kr.runGraph(ex, m64, in64, 0, T)
         stats = {}
         for key in forms:

@@ -89,10 +89,13 @@ class StageGen:
         self.tag = tag
         self.dtype = spec["dtype"]
         self.T = "float" if self.dtype == "float" else "double"
-        # type of the running sums (Kahan window sums, window reductions,
-        # regression sums): fp64 or two-float compensated fp32 in the
-        # precision forms of an fp32 module
-        self.AT = {"f64": "double", "df32": "kun::DFloat"}.get(spec.get("accum"), self.T)
+        # type of the running sums in the precision forms of an fp32 module:
+        # fp64 or two-float compensated fp32.  RT is the type of the rolling
+        # states (Kahan window sums, regression sums), AT that of the
+        # window-loop reductions; scope "rolling" upgrades only the former
+        at = {"f64": "double", "df32": "kun::DFloat"}.get(spec.get("accum"), self.T)
+        self.RT = at
+        self.AT = at if spec.get("accum_scope", "all") == "all" else self.T
         self.kname = f"kst_{tag}_{si}"
         self.bufs = spec["buffers"]
         self.slots: Dict[int, int] = {}      # module buffer id -> param slot
@@ -300,9 +303,9 @@ class StageGen:
                 decl.append(f"  {T}* __restrict__ b{i} = ({T}*)P.w[{sc}] + s;")
                 decl.append(f"  const long long st{i} = S;")
             elif k == "FastWindowedSum":
-                state.append(f"  kun::FWSum<{self.AT}> fw{i}({op['window']});")
+                state.append(f"  kun::FWSum<{self.RT}> fw{i}({op['window']});")
             elif k == "WindowedLinearRegression":
-                state.append(f"  kun::LinReg<{self.AT}, {op['window']}> lr{i};")
+                state.append(f"  kun::LinReg<{self.RT}, {op['window']}> lr{i};")
             elif k == "ExpMovingAvg":
                 init = f"kun::knan<{T}>()"
                 if len(op["in"]) == 2:

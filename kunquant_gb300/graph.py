@@ -249,14 +249,18 @@ def predefined_spec(name: str) -> dict:
     ``<base>_acc64_f32`` is the fp32 module ``<base>_f32`` with its running
     sums (Kahan window sums, two-pass window reductions, regression sums)
     accumulated in fp64, and ``<base>_comp_f32`` the same with two-float
-    compensated fp32 sums; every other op stays fp32.  ``<base>_plain_f32``
-    is the one-launch-per-op baseline form of ``<base>_f32``."""
-    for suffix, key, val in (("_acc64_f32", "accum", "f64"), ("_comp_f32", "accum", "df32"),
-                             ("_plain_f32", "form", "plain")):
+    compensated fp32 sums; every other op stays fp32.  ``<base>_mixed_f32``
+    keeps the window-loop reductions in Kahan fp32 and makes only the rolling
+    states (Kahan window sums, regression sums) two-float compensated.
+    ``<base>_plain_f32`` is the one-launch-per-op baseline form of
+    ``<base>_f32``."""
+    for suffix, sets in (("_acc64_f32", {"accum": "f64"}), ("_comp_f32", {"accum": "df32"}),
+                         ("_mixed_f32", {"accum": "df32", "accum_scope": "rolling"}),
+                         ("_plain_f32", {"form": "plain"})):
         if name.endswith(suffix):
             spec = predefined_spec(name[:-len(suffix)] + "_f32")
             spec["name"] = spec["name"] + suffix[:-4]
-            spec[key] = val
+            spec.update(sets)
             return spec
     for ext in (".json.gz", ".json"):
         p = os.path.join(GRAPH_DIR, name + ext)

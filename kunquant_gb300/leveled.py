@@ -695,11 +695,11 @@ class LeveledGen(StageGen):
         op, T = self.ops[i], self.T
         k = op["k"]
         if k == "FastWindowedSum":
-            return f"kun::FWSum<{self.AT}> fw{i}({op['window']});"
+            return f"kun::FWSum<{self.RT}> fw{i}({op['window']});"
         if k == "Accumulator":
             return f"{T} acc{i} = 0;"
         if k == "WindowedLinearRegression":
-            return f"kun::LinReg<{self.AT}, {op['window']}> lr{i};"
+            return f"kun::LinReg<{self.RT}, {op['window']}> lr{i};"
         if k == "ExpMovingAvg":
             init = f"kun::knan<{T}>()"
             if len(op["in"]) == 2:

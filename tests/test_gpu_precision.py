@@ -1,10 +1,13 @@
 """Precision of the fp32 Alpha158 forms against the reference's FP64 TS build.
 
-Four fp32 forms run on the GPU over the same seeded inputs:
+Five fp32 forms run on the GPU over the same seeded inputs:
   * ``alpha158``       -- the reference's default fp32 build: two-pass window
                           moments, Kahan window sums, fp32 regression sums;
   * ``alpha158_fast``  -- the fast-stat build: rolling moments in
                           Kahan-compensated fp32 accumulators;
+  * ``alpha158_mixed`` -- the default build with its rolling states (Kahan
+                          window sums, regression sums) in two-float
+                          compensated fp32, window loops unchanged;
   * ``alpha158_comp``  -- fp32 factor arithmetic with every running sum
                           (Kahan window sums, window reductions, regression
                           sums) in two-float compensated fp32;
@@ -26,7 +29,8 @@ from kunquant_gb300.graph import predefined_spec
 from oracle.oracle import OracleProgram
 
 FORMS = [("alpha158_f32", "alpha158"), ("alpha158_fast_f32", "alpha158_fast"),
-         ("alpha158_comp_f32", "alpha158_comp"), ("alpha158_acc64_f32", "alpha158_acc64")]
+         ("alpha158_mixed_f32", "alpha158_mixed"), ("alpha158_comp_f32", "alpha158_comp"),
+         ("alpha158_acc64_f32", "alpha158_acc64")]
 
 
 def _errors(got, want):
