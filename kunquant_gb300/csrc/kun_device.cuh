@@ -45,6 +45,11 @@ __device__ __forceinline__ T ldw(const T* __restrict__ p, long long st, long lon
     if (EDGE) return (unsigned long long)row < (unsigned long long)length ? p[row * st] : knan<T>();
     return p[row * st];
 }
+// ring row of the value `off` ticks back, given this tick's row nm (0 <= off < W)
+__device__ __forceinline__ int ring_row(int nm, int off, int W) {
+    const int r = nm - off;
+    return r < 0 ? r + W : r;
+}
 // boolean results are all-ones / all-zeros bit masks, as SIMD compares produce
 template <typename T> __device__ __forceinline__ T kmask(bool b) {
     using U = typename FpBits<T>::U;

@@ -154,9 +154,12 @@ ServePool::~ServePool() {
 static constexpr int kStepLimitMs = 20000;
 static constexpr int kStepStreams = 8;  // concurrent stage chains inside a step
 
+// graph size buckets: powers of 4 from lo, capped at hi (a step of n uses
+// the graph of the first bucket >= n; its kernels take the exact counts
+// from the device table)
 static long long bucket(long long n, long long lo, long long hi) {
     long long b = lo;
-    while (b < n) b <<= 1;
+    while (b < n && b < hi) b <<= 2;
     return b < hi ? b : hi;
 }
 
@@ -208,7 +211,25 @@ static KunStatus build_serve_graph(ServePool *p, long long nb, int sb, cudaGraph
 struct StepShape {
     int nsess = 0;
     long long n = 0, lo = 0, hi = 0;
+    // column runs [first, second) of the step's sessions, merged where adjacent
+    std::vector<std::pair<long long, long long>> runs;
 };
+
+static KunStatus graph_for(ServePool *p, long long nb, int sb, cudaGraphExec_t *out);
+
+// the graph of a (stocks, sessions) bucket, built on first use (gpu_mu held)
+static KunStatus graph_for(ServePool *p, long long nb, int sb, cudaGraphExec_t *out) {
+    auto key = std::make_pair(nb, sb);
+    auto g = p->graphs.find(key);
+    if (g == p->graphs.end()) {
+        cudaGraphExec_t ge = nullptr;
+        KunStatus rs = build_serve_graph(p, nb, sb, &ge);
+        if (rs != KUN_SUCCESS) return rs;
+        g = p->graphs.emplace(key, ge).first;
+    }
+    *out = g->second;
+    return KUN_SUCCESS;
+}
 
 static KunStatus run_step(ServePool *p, const StepShape &sh, const void *dev_in, void *dev_out) {
     std::lock_guard<std::mutex> g_lk(p->gpu_mu);
@@ -218,30 +239,31 @@ static KunStatus run_step(ServePool *p, const StepShape &sh, const void *dev_in,
     cudaMemcpyAsync(p->d_table, p->h_table, (2 * p->max_sessions + 4) * sizeof(int32_t), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(p->d_table + p->tick_off, p->h_table + p->tick_off, sh.nsess * sizeof(long long),
                     cudaMemcpyHostToDevice, st);
-    // the column span [lo, hi) of every input row, one 2D copy
-    size_t pitch = (size_t)p->cap * elem, span = (size_t)(sh.hi - sh.lo) * elem;
-    const char *src_in = (const char *)(dev_in ? dev_in : p->h_in) + (size_t)sh.lo * elem;
-    cudaMemcpy2DAsync((char *)p->d_in + (size_t)sh.lo * elem, pitch, src_in, pitch, span, p->in_bufs.size(),
-                      dev_in ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
-    long long nb = bucket(sh.n, 256, p->cap);
-    int sb = (int)bucket(sh.nsess, 1, p->max_sessions);
-    auto key = std::make_pair(nb, sb);
-    auto g = p->graphs.find(key);
-    if (g == p->graphs.end()) {
-        cudaGraphExec_t ge = nullptr;
-        KunStatus rs = build_serve_graph(p, nb, sb, &ge);
-        if (rs != KUN_SUCCESS) return rs;
-        g = p->graphs.emplace(key, ge).first;
-    }
-    cudaError_t e = cudaGraphLaunch(g->second, st);
+    // every input and output row moves as 2D copies: one over the column
+    // span [lo, hi) when the step's sessions fill most of it, else one per
+    // run of adjacent sessions
+    size_t pitch = (size_t)p->cap * elem;
+    std::vector<std::pair<long long, long long>> whole{{sh.lo, sh.hi}};
+    const auto &runs = (sh.n * 2 >= sh.hi - sh.lo || sh.runs.empty()) ? whole : sh.runs;
+    const char *h_in = (const char *)(dev_in ? dev_in : p->h_in);
+    for (const auto &r : runs)
+        cudaMemcpy2DAsync((char *)p->d_in + (size_t)r.first * elem, pitch, h_in + (size_t)r.first * elem, pitch,
+                          (size_t)(r.second - r.first) * elem, p->in_bufs.size(),
+                          dev_in ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, st);
+    cudaGraphExec_t ge = nullptr;
+    KunStatus rs = graph_for(p, bucket(sh.n, 256, p->cap), (int)bucket(sh.nsess, 4, p->max_sessions), &ge);
+    if (rs != KUN_SUCCESS) return rs;
+    cudaError_t e = cudaGraphLaunch(ge, st);
     if (e != cudaSuccess) {
         set_error("serving step launch failed: %s", cudaGetErrorString(e));
         return KUN_CUDA_ERROR;
     }
     if (!p->out_bufs.empty()) {
-        char *dst_out = (char *)(dev_out ? dev_out : p->h_out) + (size_t)sh.lo * elem;
-        cudaMemcpy2DAsync(dst_out, pitch, (const char *)p->d_out + (size_t)sh.lo * elem, pitch, span,
-                          p->out_bufs.size(), dev_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st);
+        char *h_out = (char *)(dev_out ? dev_out : p->h_out);
+        for (const auto &r : runs)
+            cudaMemcpy2DAsync(h_out + (size_t)r.first * elem, pitch, (const char *)p->d_out + (size_t)r.first * elem,
+                              pitch, (size_t)(r.second - r.first) * elem, p->out_bufs.size(),
+                              dev_out ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st);
     }
     // wait with a limit, so a step that never finishes is reported instead
     // of blocking the loop and every client
@@ -297,6 +319,19 @@ static KunStatus prepare_step(ServePool *p, int nsess, const int64_t *sids, std:
         hi = std::max(hi, s.stock0 + s.len);
     }
     off[nsess] = (int32_t)n;
+    // column runs of the selected sessions
+    sh.runs.clear();
+    {
+        std::vector<std::pair<long long, long long>> cols(nsess);
+        for (int k = 0; k < nsess; k++) cols[k] = {sel[k]->stock0, sel[k]->stock0 + sel[k]->len};
+        std::sort(cols.begin(), cols.end());
+        for (const auto &c : cols) {
+            if (!sh.runs.empty() && sh.runs.back().second == c.first)
+                sh.runs.back().second = c.second;
+            else
+                sh.runs.push_back(c);
+        }
+    }
     cnt[0] = nsess;
     cnt[1] = (int32_t)n;
     cnt[2] = longest;
@@ -561,6 +596,21 @@ KUN_EXPORT KunStatus kunServeStart(KunServePoolHandle pool, int batch_window_us)
     std::lock_guard<std::mutex> lk(p->mu);
     if (p->running) return KUN_SUCCESS;
     p->batch_window_us = batch_window_us > 0 ? batch_window_us : 0;
+    // every size bucket's graph is built now, so no step of the loop waits
+    // for a graph capture
+    {
+        std::lock_guard<std::mutex> g_lk(p->gpu_mu);
+        cudaSetDevice(p->ex->device);
+        for (long long nb = 256;; nb = std::min<long long>(nb << 2, p->cap)) {
+            for (int sb = 4;; sb = std::min(sb << 2, p->max_sessions)) {
+                cudaGraphExec_t ge;
+                KunStatus rs = graph_for(p, std::min<long long>(nb, p->cap), std::min(sb, p->max_sessions), &ge);
+                if (rs != KUN_SUCCESS) return rs;
+                if (sb >= p->max_sessions) break;
+            }
+            if (nb >= p->cap) break;
+        }
+    }
     p->failed = KUN_SUCCESS;
     p->running = true;
     p->loop = std::thread(serve_loop, p);

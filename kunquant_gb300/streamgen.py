@@ -53,14 +53,24 @@ class StreamGen(StageGen):
     def read_at(self, src: int, texpr: str) -> str:
         raise RuntimeError("stream kernels read rings by offset")
 
-    def window_read(self, src: int, off) -> str:
+    def window_read(self, src: int, off, max_off=None) -> str:
+        """Row `off` ticks back in the ring of `src` (NaN before tick 0).  When
+        `off` is known to stay below the ring depth W (a constant, or a loop
+        index bounded by `max_off`), the row is nm - off wrapped once, from
+        the tick's ring position nm = n % W computed once per kernel."""
         W = self.ring_window(src)
+        bound = max_off if max_off is not None else (off if isinstance(off, int) else None)
+        if bound is not None and 0 <= bound < W:
+            self.ring_ws.add(W)
+            return (f"((nc >= (int)({off})) ? r{src}[(long long)kun::ring_row(nm{W}, (int)({off}), {W}) * S] "
+                    f": kun::knan<{self.T}>())")
         return (f"((n - (long long)({off}) >= 0) ? r{src}[((n - (long long)({off})) % {W}) * S] "
                 f": kun::knan<{self.T}>())")
 
     def cur_read(self, src: int) -> str:
         W = self.ring_window(src)
-        return f"r{src}[(n % {W}) * S]"
+        self.ring_ws.add(W)
+        return f"r{src}[(long long)nm{W} * S]"
 
     # --------------------------------------------------------------- state
     def _state_fields(self) -> Dict[int, Tuple[List[str], List[str]]]:
@@ -159,12 +169,14 @@ class StreamGen(StageGen):
                 stores.append(f"  {src} = {tgt};")
         # ops of one tick (CodegenCpp.py:189-307 with length 1)
         self.lines = []
+        self.ring_ws = set()
         loops = self._loops()
         for i, op in enumerate(ops):
             if op.get("p", -1) >= 0:
                 continue
             self._emit(i, loops)
         body = "\n".join(self.lines)
+        ring_pos = "\n".join(f"  const int nm{W} = (int)(n % {W});" for W in sorted(self.ring_ws))
         pstruct = f"P_{self.kname}"
         nslots = max(1, len(self.slots))
         src = _SEG_HELPER + f"""
@@ -191,6 +203,10 @@ __global__ void __launch_bounds__(KUN_TS_THREADS) {self.kname}(const {pstruct} P
   const long long S = P.S;
   const long long t = 0;  // the reference's row index within a one-row run
   (void)t;
+  // ticks so far (capped) and this tick's row in each ring depth
+  const int nc = n < (1LL << 30) ? (int)n : (1 << 30);
+  (void)nc;
+{ring_pos}
   {T}* __restrict__ st = P.st + s;
   int32_t* __restrict__ si = P.si + s;
   (void)st; (void)si;
@@ -284,12 +300,15 @@ extern "C" int {self.kname}_init(const KunGpuStageArgs* a, void* stream) {{
             w, seg = op["window"], op.get("segment_end", 0)
             for r in own:
                 L.append(f"{ind}{self.reduction_decl(r)}")
+            # unrolled so that the ring loads of several iterations are in
+            # flight together: one thread walks the window alone
+            L.append(f"{ind}#pragma unroll 8")
             L.append(f"{ind}for (int iter = {w - 1}; iter >= {seg}; --iter) {{")
             bind = ind + "  "
             for j in body:
                 bo = ops[j]
                 if bo["k"] == "IterValue":
-                    L.append(f"{bind}const {T} v{j} = {self.window_read(bo['in'][1], 'iter')};")
+                    L.append(f"{bind}const {T} v{j} = {self.window_read(bo['in'][1], 'iter', w - 1)};")
                 elif bo["k"] == "WindowLoopIndex":
                     L.append(f"{bind}const {T} v{j} = ({T})({bo.get('loop_window', w)} - 1 - iter);")
                 elif not self.emit_simple(j, bind, fplan):
