@@ -2,8 +2,8 @@
 // layout).
 //  - Rank (cpp/Kun/Rank.hpp:13-57): the row's non-NaN values are sorted by a
 //    register/shuffle/shared-memory bitonic network over order-preserving
-//    integer keys (NaNs sort last), then every stock binary-searches its
-//    equal range;
+//    integer keys (NaNs sort last), or for long rows an 8-bit LSD radix sort;
+//    every stock then finds its equal range;
 //    out = T(sum) / T(cnt) / T(n) with the integer rank sum of the range.
 //  - Scale (cpp/Kun/Scale.hpp:14-46): the sum of |x| over non-NaN stocks in
 //    stock order (sequential, as the reference adds), then x / sum.
@@ -175,34 +175,44 @@ __device__ __forceinline__ void rank_one_row(const T *__restrict__ row, T *__res
     rank_from_sorted<T>(row, orow, S, n, [&](int p) { return SK::dec(keys[(p % ITEMS) * nt + p / ITEMS]); });
 }
 
-// Rank of one row by LSD radix sort (4-bit digits, stable), for long rows
+// Rank of one row by LSD radix sort (8-bit digits, stable), for long rows
 // where the bitonic network's P log^2 P exchanges cost more than the digit
-// passes.  blockDim.x must be kRankThreads; thread t holds positions
-// [t*ITEMS, (t+1)*ITEMS).  Only the non-NaN values are sorted, each with its
-// stock index, and only the digits in which they differ are passed over.  The
-// ranks then come from the sorted run of equal values around each position
-// (two block scans) instead of binary searches.  Shared memory: keys, 16 x
-// kRankThreads 32-bit digit counters and 16-bit stock indices, each skewed by
-// one slot every 32 so that counting, scan and reloads are conflict-free.
+// passes.  blockDim.x must be kRankThreads.  Between passes the values sit in
+// layout order: warp w, item e, lane l holds position w*32*ITEMS + e*32 + l.
+// Only the non-NaN values are sorted, each with its stock index, and only
+// the digits in which they differ are passed over.  A pass counts digits per
+// warp (peers of a digit found with match.any, so an item's offset is the
+// warp's running count of its digit plus its peers in lower lanes), scans
+// the counts in (digit, warp) order and scatters.  The ranks then come from
+// the sorted run of equal values around each position (two block scans)
+// instead of binary searches.  Shared memory: keys and 16-bit stock indices
+// (skewed by one slot every 32), and kRankThreads/32 x 257 digit counters.
+constexpr int kRadixHistStride = 257;  // 256 digits + 1: warps' rows skewed by one bank
+__host__ __device__ inline int radix_hist_slots() { return (kRankThreads / 32) * kRadixHistStride; }
+
 template <typename T, int ITEMS>
 __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T *__restrict__ orow, long long S,
-                                                   typename SortKey<T>::K *keys, uint32_t *counters,
+                                                   typename SortKey<T>::K *keys, uint32_t *hist,
                                                    uint16_t *idx, int *cnt_warp) {
     using SK = SortKey<T>;
     using K = typename SK::K;
     constexpr int NT = kRankThreads;
+    constexpr int NW = NT / 32;
+    static_assert(NT == 1024, "the digit-count scan gives each thread 8 of 256 x 32 counts");
     constexpr int BITS = (int)sizeof(K) * 8;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    __shared__ int warp_tot[NT / 32], warp_tot2[NT / 32];
-    __shared__ K red_or[NT / 32], red_and[NT / 32];
+    const unsigned lt_mask = (1u << lane) - 1u;
+    __shared__ int warp_tot[NW], warp_tot2[NW];
+    __shared__ K red_or[NW], red_and[NW];
     K r[ITEMS];
     uint16_t ix[ITEMS];
     bool real[ITEMS];
     int local = 0;
     K o_or = 0, o_and = ~K(0);
+    const int wbase = warp * 32 * ITEMS + lane;  // layout position of item 0
 #pragma unroll
     for (int e = 0; e < ITEMS; e++) {
-        const int i = tid * ITEMS + e;
+        const int i = wbase + e * 32;
         real[e] = false;
         r[e] = SK::kMax;
         ix[e] = (uint16_t)i;
@@ -232,7 +242,7 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
     __syncthreads();
     int n = 0;
     K orv = 0, andv = ~K(0);
-    for (int w = 0; w < NT / 32; w++) {
+    for (int w = 0; w < NW; w++) {
         n += cnt_warp[w];
         orv |= red_or[w];
         andv &= red_and[w];
@@ -246,57 +256,72 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
     K todo = orv ^ andv;
     if (todo == 0) todo = 1;
     int last_shift = 0;
-    for (int sh = 0; sh < BITS; sh += 4)
-        if ((todo >> sh) & 15) last_shift = sh;
-    for (int shift = 0; shift < BITS; shift += 4) {
-        if (((todo >> shift) & 15) == 0) continue;
-#pragma unroll
-        for (int d = 0; d < 16; d++) counters[skew(d * NT + tid)] = 0;
-        uint16_t mine[ITEMS];
+    for (int sh = 0; sh < BITS; sh += 8)
+        if ((todo >> sh) & 255) last_shift = sh;
+    uint32_t *my_hist = hist + warp * kRadixHistStride;
+    for (int shift = 0; shift < BITS; shift += 8) {
+        if (((todo >> shift) & 255) == 0) continue;
+        for (int d = lane; d < 256; d += 32) my_hist[d] = 0;
+        __syncwarp();
+        // per-warp counts; off[e] = the item's place among its warp's items
+        // of the same digit, in layout order
+        uint16_t off[ITEMS];
 #pragma unroll
         for (int e = 0; e < ITEMS; e++) {
-            mine[e] = 0;
-            if (real[e]) {
-                const int d = (int)((r[e] >> shift) & 15);
-                mine[e] = (uint16_t)(counters[skew(d * NT + tid)]++);
+            const int d = real[e] ? (int)((r[e] >> shift) & 255) : 256;
+            const unsigned peers = __match_any_sync(0xffffffffu, d);
+            const int leader = __ffs(peers) - 1;
+            uint32_t base = 0;
+            if (lane == leader && d < 256) {
+                base = my_hist[d];
+                my_hist[d] = base + (uint32_t)__popc(peers);
             }
+            base = __shfl_sync(0xffffffffu, base, leader);
+            off[e] = (uint16_t)(base + (uint32_t)__popc(peers & lt_mask));
+            __syncwarp();
         }
         __syncthreads();
-        // exclusive scan of the counters in (digit, thread) order: thread t
-        // takes the 16 consecutive entries [16t, 16t + 16)
-        int sum = 0;
+        // exclusive scan of the counts in (digit, warp) order: thread t takes
+        // the 8 entries of digit t/4, warps (t%4)*8 .. +8
+        {
+            const int d = tid >> 2, w0 = (tid & 3) * 8;
+            uint32_t c[8];
+            int sum = 0;
 #pragma unroll
-        for (int q = 0; q < 16; q++) sum += counters[skew(tid * 16 + q)];
-        int incl = sum;
-        for (int o = 1; o < 32; o <<= 1) {
-            int v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= o) incl += v;
-        }
-        if (lane == 31) warp_tot[warp] = incl;
-        __syncthreads();
-        if (tid < 32) {
-            int v = warp_tot[tid];
-            int x = v;
+            for (int j = 0; j < 8; j++) {
+                c[j] = hist[(w0 + j) * kRadixHistStride + d];
+                sum += (int)c[j];
+            }
+            int incl = sum;
             for (int o = 1; o < 32; o <<= 1) {
-                int y = __shfl_up_sync(0xffffffffu, x, o);
-                if (tid >= o) x += y;
+                int v = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += v;
             }
-            warp_tot[tid] = x - v;  // exclusive
-        }
-        __syncthreads();
-        int run = warp_tot[warp] + incl - sum;
+            if (lane == 31) warp_tot[warp] = incl;
+            __syncthreads();
+            if (tid < 32) {
+                int v = tid < NW ? warp_tot[tid] : 0;
+                int x = v;
+                for (int o = 1; o < 32; o <<= 1) {
+                    int y = __shfl_up_sync(0xffffffffu, x, o);
+                    if (tid >= o) x += y;
+                }
+                if (tid < NW) warp_tot[tid] = x - v;  // exclusive
+            }
+            __syncthreads();
+            uint32_t run = (uint32_t)(warp_tot[warp] + incl - sum);
 #pragma unroll
-        for (int q = 0; q < 16; q++) {
-            const int v = (int)counters[skew(tid * 16 + q)];
-            counters[skew(tid * 16 + q)] = (uint32_t)run;
-            run += v;
+            for (int j = 0; j < 8; j++) {
+                hist[(w0 + j) * kRadixHistStride + d] = run;
+                run += c[j];
+            }
         }
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < ITEMS; e++) {
             if (real[e]) {
-                const int d = (int)((r[e] >> shift) & 15);
-                const int pos = skew((int)counters[skew(d * NT + tid)] + mine[e]);
+                const int d = (int)((r[e] >> shift) & 255);
+                const int pos = skew((int)my_hist[d] + off[e]);
                 keys[pos] = r[e];
                 idx[pos] = ix[e];
             }
@@ -305,7 +330,7 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
         if (shift != last_shift) {
 #pragma unroll
             for (int e = 0; e < ITEMS; e++) {
-                const int p = tid * ITEMS + e;
+                const int p = wbase + e * 32;
                 real[e] = p < n;
                 if (real[e]) {
                     r[e] = keys[skew(p)];
@@ -393,7 +418,7 @@ template <typename T>
 inline size_t rank_smem_bytes(int P) {
     using K = typename SortKey<T>::K;
     size_t keys = ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16;
-    return P >= kRadixMinP ? keys + ((size_t)skew(16 * kRankThreads) + 1) * sizeof(uint32_t) +
+    return P >= kRadixMinP ? keys + (size_t)radix_hist_slots() * sizeof(uint32_t) +
                                  (size_t)rank_key_slots(P) * sizeof(uint16_t)
                            : keys;
 }
@@ -406,7 +431,7 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ 
     __shared__ int cnt_warp[kRankThreads / 32];
     K *keys = reinterpret_cast<K *>(smem_raw);
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
-    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + skew(16 * kRankThreads) + 1);
+    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
     for (long long t = blockIdx.x; t < length; t += gridDim.x) {
         if (P >= kRadixMinP)
             rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, idx, cnt_warp);
@@ -433,7 +458,7 @@ __global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restric
     while (Pk < len) Pk <<= 1;
     K *keys = reinterpret_cast<K *>(smem_raw);
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
-    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + skew(16 * kRankThreads) + 1);
+    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
     if (Pk >= kRadixMinP)
         rank_one_row_radix<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys, counters,
                                      idx, cnt_warp);
