@@ -262,6 +262,39 @@ def serving(nsess=256, rate=20000.0, seconds=3.0, warm=250, seed=3):
                                         "max_session_ticks_per_s": 1.0 / per_call}}
 
 
+def serve_steps_main(args):
+    """Serving steps driven by the caller (no request loop): `--sessions`
+    sessions of the Alpha101 stream module (sizes log-uniform in [100, 5000],
+    the serving workload's first ones) advance one tick together per step;
+    CUDA-event time per step after `--warmup` steps."""
+    import torch
+    from kunquant_gb300 import runner as kr
+    from kunquant_gb300 import serve
+    torch.cuda.set_device(0)
+    mod = kr.Library.predefined("alpha101_stream_f32").getModule("alpha101_stream")
+    rng = np.random.default_rng(3)
+    sizes = np.exp(rng.uniform(np.log(100), np.log(5000), 256)).astype(int)[:args.sessions]
+    cap = int(sizes.sum())
+    ex = kr.createSingleThreadExecutor()
+    pool = serve.ServePool(ex, mod, capacity_stocks=cap, max_sessions=256, max_session_stocks=5000, start=False)
+    sess = [pool.open(int(k)) for k in sizes]
+    for s in sess:
+        for k in mod.getInputNames():
+            s.inputs[k][:] = rng.uniform(10, 100, s.num_stocks).astype(np.float32)
+    for _ in range(args.warmup):
+        pool.step(sess)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pool.step(sess)
+    dt = (time.perf_counter() - t0) / args.steps
+    pool.shutdown()
+    print(json.dumps({"metric": "ms per serving step", "value": dt * 1e3, "unit": "ms", "higher_is_better": False,
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "data": "synthetic",
+                      "config": {"workload": f"alpha101_stream_f32 serving step, {args.sessions} sessions, "
+                                             f"{cap} stocks, caller-driven (kunServeStep)"}}))
+
+
 def universes_main(args):
     """Many universes of uneven size: `--universes` universes of Alpha158 fp32
     with S log-uniform in [37, 6000] stocks and T uniform in [250, 5000] days
@@ -418,7 +451,9 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="alpha158", choices=sorted(WORKLOADS) + ["universes", "precision"])
+    ap.add_argument("--workload", default="alpha158",
+                    choices=sorted(WORKLOADS) + ["universes", "precision", "serve_steps"])
+    ap.add_argument("--sessions", type=int, default=16, help="sessions of the 'serve_steps' workload")
     ap.add_argument("--report", default=None, help="precision workload: write the per-factor table here")
     ap.add_argument("--stocks", type=int, default=None)
     ap.add_argument("--days", type=int, default=None)
@@ -429,6 +464,11 @@ def main():
     ap.add_argument("--universes", type=int, default=48, help="universes of the 'universes' workload")
     ap.add_argument("--streams", type=int, default=8, help="CUDA streams for concurrent stages")
     args = ap.parse_args()
+    if args.workload == "serve_steps":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "serve_steps times the GPU serving pool only"}))
+            return
+        return serve_steps_main(args)
     if args.workload == "precision":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the precision workload compares the GPU forms "

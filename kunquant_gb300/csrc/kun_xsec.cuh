@@ -400,15 +400,31 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
     __syncthreads();
     const int start_in = max(fex, warp_tot[warp]);
     const int end_in = min(bex, warp_tot2[warp]);
+    T res[ITEMS];
+    int sidx[ITEMS];
 #pragma unroll
     for (int e = 0; e < ITEMS; e++) {
         const int p = p0 + e;
+        sidx[e] = -1;
         if (p < n) {
             const long long start = max(st[e], start_in);
             const long long end = min(en[e], end_in);
             const long long sum = (start + end + 1) * (end - start) / 2;
-            orow[idx[skew(p)]] = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
+            res[e] = kdiv(kdiv((T)sum, (T)(end - start)), (T)n);
+            sidx[e] = idx[skew(p)];
         }
+    }
+    // the results go to shared memory by stock index (over the keys, no
+    // longer needed), then out in one coalesced pass over the row
+    __syncthreads();
+    T *out_s = reinterpret_cast<T *>(keys);
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++)
+        if (sidx[e] >= 0) out_s[sidx[e]] = res[e];
+    __syncthreads();
+    for (long long i = tid; i < S; i += NT) {
+        const T x = row[i];
+        orow[i] = x == x ? out_s[i] : knan<T>();
     }
     __syncthreads();
 }
