@@ -320,7 +320,11 @@ KUN_EXPORT int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle mod, int 
         float best = -1.f;
         // times the stage with shape (t, b); keeps it when fastest so far
         auto run = [&]() -> bool {
-            br.host_off = 0;  // earlier trials of this stage are complete below
+            // the staging area is reused from its start: the copies of every
+            // earlier launch (this stage's trials, and the untuned stages
+            // enqueued before it) must have left it
+            if (cudaStreamSynchronize(st) != cudaSuccess) return false;
+            br.host_off = 0;
             if (batch_stage(br, si, st, t.data(), b.data(), launches) != KUN_SUCCESS) return false;
             cudaEventRecord(e0, st);
             for (int r = 0; r < reps; r++) {

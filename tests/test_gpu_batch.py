@@ -83,3 +83,17 @@ def test_more_universes_than_one_group():
     for i in (0, 1, 255, 256, 299):
         want = _singles(ex, mod, [unis[i]])[0]
         assert not compare_exact(got[i], want), f"universe {i}"
+
+
+@pytest.mark.gpu
+def test_batch_rank_long_and_short_rows():
+    """Alpha101 in a batch with a universe long enough for the radix Rank
+    (2100 stocks) beside short ones (bitonic network): every universe
+    bit-identical to its own run."""
+    mod = kr.Library.predefined("alpha101_f32").getModule("alpha101")
+    unis = _universes([(2100, 300), (37, 260), (700, 280)], seed=12)
+    ex = kr.createSingleThreadExecutor()
+    want = _singles(ex, mod, unis)
+    got = _cpu(kr.runGraphBatch(ex, mod, [dev for _, dev in unis]))
+    for i in range(len(unis)):
+        assert not compare_exact(got[i], want[i]), f"universe {i}"

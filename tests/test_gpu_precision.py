@@ -93,3 +93,7 @@ def test_alpha158_precision_vs_fp64():
     comp = stats["alpha158_comp"]
     assert all(comp[f][1] <= 1e-5 for f in names), [f for f in names if comp[f][1] > 1e-5]
     assert sum(comp[f][2] for f in names) == 0
+    # compensating only the rolling states already holds every median
+    mixed = stats["alpha158_mixed"]
+    assert all(mixed[f][1] <= 1e-5 for f in names), [f for f in names if mixed[f][1] > 1e-5]
+    assert sum(mixed[f][2] for f in names) == 0
