@@ -70,3 +70,36 @@ def test_interior_reads_stay_in_bounds(key, tmp_path):
                        src)
     assert tiles
     assert all(int(d) % 4 == 0 for d in tiles), tiles
+
+
+RING = re.compile(r"kun::ring_row\(nm(\d+), \(int\)\((\w+)\), (\d+)\)")
+
+
+@pytest.mark.parametrize("key", ["alpha101_stream_f32", "alpha158_stream_f32"])
+def test_stream_ring_rows_wrap_once(key, tmp_path):
+    """Stream kernels find a ring row as nm - off wrapped once (nm = n % W):
+    right only for 0 <= off < W.  Every such read in the generated sources
+    has a constant offset or a window-loop index below its ring depth, and
+    names the ring position of its own depth."""
+    spec = predefined_spec(key)
+    paths = codegen.generate_module(spec, str(tmp_path), tag=spec["name"])
+    src = "".join(open(p).read() for p in paths)
+    n = 0
+    for m in RING.finditer(src):
+        nm_w, off, W = int(m.group(1)), m.group(2), int(m.group(3))
+        assert nm_w == W, m.group(0)
+        if off == "iter":
+            loops = list(LOOP.finditer(src, 0, m.start()))
+            assert loops, m.group(0)
+            hi = int(loops[-1].group(1))
+            assert 0 <= int(loops[-1].group(2)) and hi < W, f"{m.group(0)} inside a loop from {hi}"
+        else:
+            assert 0 <= int(off) < W, m.group(0)
+        n += 1
+    assert n > 100
+    # every ring position a kernel uses is declared in it
+    for k in re.finditer(r"__global__ void __launch_bounds__\(KUN_TS_THREADS\) (\w+)\(", src):
+        end = src.find("\n}\n", k.end())
+        body = src[k.end():end]
+        for w in set(re.findall(r"\bnm(\d+)\b", body)):
+            assert f"const int nm{w} = (int)(n % {w});" in body, f"{k.group(1)}: nm{w}"
