@@ -112,26 +112,35 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except Exception:
             self.proc.kill()
-        rows = []
         with open(self.path) as f:
-            for line in f:
-                parts = [p.strip() for p in line.split(",")]
-                if len(parts) >= 9:
-                    rows.append(parts)
+            lines = f.readlines()
         os.unlink(self.path)
-        if not rows:
-            return None
-        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
-        reasons = set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
-            for n, v in zip(names, r[5:9]):
-                if v.lower() == "active":
-                    reasons.add(n)
-        return {"sm_mhz": float(np.median(sm)) if sm else None,
-                "sm_max_mhz": max(mx) if mx else None,
-                "reasons": sorted(reasons), "samples": len(rows)}
+        return parse_clocks(lines)
+
+
+def parse_clocks(lines):
+    """Summary of nvidia-smi rows (index, clocks.sm, clocks.max.sm, power,
+    reasons.active, hw_slowdown, hw_thermal_slowdown, sw_thermal_slowdown,
+    sw_power_cap): median SM clock, max clock and the throttle reasons seen
+    active in any sample."""
+    rows = []
+    for line in lines:
+        parts = [p.strip() for p in line.split(",")]
+        if len(parts) >= 9:
+            rows.append(parts)
+    if not rows:
+        return None
+    sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+    mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+    reasons = set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for r in rows:
+        for n, v in zip(names, r[5:9]):
+            if v.lower() == "active":
+                reasons.add(n)
+    return {"sm_mhz": float(np.median(sm)) if sm else None,
+            "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons), "samples": len(rows)}
 
 
 def cpu_reference(workload: dict, steps: int, warmup: int, seconds_target: float = 15.0):

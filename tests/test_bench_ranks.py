@@ -78,3 +78,29 @@ def test_factor_errors_matches_numpy():
     assert got[2] == 2
     assert got[0] == pytest.approx(rel.max(), rel=1e-12)
     assert got[1] == pytest.approx(np.sort(rel)[(rel.size - 1) // 2], rel=1e-12)
+
+
+def test_clock_summary():
+    """The clocks object of the bench line: median SM clock under load, the
+    maximum, and every throttle reason seen active."""
+    sys.path.insert(0, REPO)
+    import bench
+    rows = ["0, 2070, 2070, 900.5, 0x0, Not Active, Not Active, Not Active, Not Active\n",
+            "0, 1950, 2070, 1390.0, 0x4, Not Active, Not Active, Not Active, Active\n",
+            "0, 2040, 2070, 1200.0, 0x0, Not Active, Not Active, Not Active, Not Active\n",
+            "garbage line\n"]
+    c = bench.parse_clocks(rows)
+    assert c == {"sm_mhz": 2040.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert bench.parse_clocks([]) is None
+
+
+def test_stage_bytes_counts_distinct_series():
+    """Algorithmic bytes of a stage: its distinct input and output series,
+    each S x T elements."""
+    sys.path.insert(0, REPO)
+    import bench
+    from kunquant_gb300.graph import predefined_spec
+    spec = predefined_spec("alpha158_f32")
+    for si, st in enumerate(spec["stages"]):
+        n = len(set(st["in"]) | set(st["out"]))
+        assert bench.stage_bytes(spec, si, 10, 20, 4) == n * 10 * 20 * 4
