@@ -67,6 +67,19 @@ def job_value(world: int, stocks: int, days: int, ms: float) -> float:
     return world * stocks * days / (ms / 1e3)
 
 
+def relaunch_replicas(n: int) -> int:
+    """`--gpus N` without a launcher: start N ranks of this same command
+    under torch.distributed.run (one process per GPU, rendezvous on
+    127.0.0.1); rank 0 prints the line.  Returns the launcher's exit code."""
+    import socket
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", str(n),
+           "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.abspath(__file__)] + sys.argv[1:]
+    return subprocess.call(cmd, cwd=REPO)
+
+
 def _dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -487,6 +500,8 @@ def main():
     ap.add_argument("--universes", type=int, default=48, help="universes of the 'universes' workload")
     ap.add_argument("--streams", type=int, default=8, help="CUDA streams for concurrent stages")
     args = ap.parse_args()
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        sys.exit(relaunch_replicas(args.gpus))
     if args.workload == "serve_steps":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "serve_steps times the GPU serving pool only"}))
@@ -518,7 +533,7 @@ def main():
         if rank != 0:
             return
         ref = cpu_reference(wl, args.steps, args.warmup)
-        line = {"metric": metric, "value": ref["value"], "unit": "stock-days/s", "n_gpus": args.gpus,
+        line = {"metric": metric, "value": ref["value"], "unit": "stock-days/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ref["s_per_step"] * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": config, "impl": "reference",

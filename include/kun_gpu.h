@@ -207,7 +207,13 @@ KunStatus kunAggregrate(KunExecutorHandle exec, int n, const void *const *inputs
  * call on each device does a one-time set-up (address lookup of the static
  * array) and should come before any stream capture on that device.  All calls
  * on a device share the array: calls whose GPU work overlaps race and must be
- * ordered by the caller (one stream, or events). */
+ * ordered by the caller (one stream, or events).
+ * Fixed cost: the array is device memory of the translation unit that holds
+ * it.  With CUDA's default lazy module loading it is reserved on a device at
+ * the first kunRunGraphNoAlloc call there; with CUDA_MODULE_LOADING=EAGER,
+ * every process that loads libkungpu.so holds it on every device it uses,
+ * until exit, whether it calls this function or not.  Memory budgets (the
+ * serving pool's hbm budget, for one) should be measured after that. */
 #define KUN_NOALLOC_SCRATCH_BYTES (64u << 20)
 KunStatus kunRunGraphNoAlloc(KunModuleHandle m, KunBufferNameMapHandle buffers, size_t num_stocks,
                              size_t total_time, size_t cur_time, size_t length, void *cuda_stream);

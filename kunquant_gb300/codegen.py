@@ -569,6 +569,7 @@ template <> struct LogTables<{T}> {{
     init_fn = ["nullptr"] * n_stages
     extern_init = []
     kinfo: Dict[int, List[int]] = {}
+    imax: Dict[int, List[int]] = {}
     files: List[List[str]] = []
     cur: List[str] = []
     for si in range(n_stages):
@@ -577,6 +578,9 @@ template <> struct LogTables<{T}> {{
         scratch_counts[si] = nscr
         kernel_counts[si] = nk
         state_t[si], state_i[si] = getattr(g, "state_t_vars", 0), getattr(g, "state_i_vars", 0)
+        if state_i[si]:
+            imax[si] = list(g.state_i_max)
+            assert len(imax[si]) == state_i[si]
         if getattr(g, "has_init", False):
             init_fn[si] = f"kst_{tag}_{si}_init"
             extern_init.append(si)
@@ -605,6 +609,8 @@ template <> struct LogTables<{T}> {{
         lines.append(f'extern "C" size_t kst_{tag}_{si}_prepare(const KunGpuStageArgs*, int, void*);')
         lines.append(f'extern "C" int kst_{tag}_{si}_launch_group(const KunGpuStageArgs*, int, const void*, void*);')
         lines.append(f"static const int32_t st{si}_kinfo[] = {{{', '.join(str(v) for v in ki)}}};")
+    for si, mx in imax.items():
+        lines.append(f"static const int32_t st{si}_imax[] = {{{', '.join(str(v) for v in mx)}}};")
     for si, st in enumerate(spec["stages"]):
         for key in ("in", "out", "deps"):
             vals = st.get(key, []) or []
@@ -618,6 +624,7 @@ template <> struct LogTables<{T}> {{
                      f"{len(st['out'])}, st{si}_out, {len(st.get('deps', []))}, st{si}_deps, "
                      f"{st.get('pending', 0)}, {scratch_counts[si]}, 0, kst_{tag}_{si}_launch, {kernel_counts[si]}, "
                      f"{state_t[si]}, {state_i[si]}, {init_fn[si]}, "
+                     + (f"st{si}_imax, " if si in imax else "nullptr, ")
                      + (f"st{si}_kinfo, kst_{tag}_{si}_prepare, kst_{tag}_{si}_launch_group}},"
                         if si in kinfo else "nullptr, nullptr, nullptr},"))
     lines.append("};")

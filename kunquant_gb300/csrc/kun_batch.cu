@@ -159,7 +159,6 @@ static KunStatus batch_stage(BatchRun &br, int si, cudaStream_t st, const int32_
         a.total_time = jb.total_time;
         a.start = jb.cur_time;
         a.length = jb.length;
-        a.error_flag = ex->d_error;
         if (tile) {
             a.tune_tile = tile;
             a.tune_block = block;
@@ -254,6 +253,7 @@ KUN_EXPORT KunStatus kunRunGraphBatch(KunExecutorHandle exec, KunModuleHandle mo
     if (!ex) return KUN_INVALID_ARGUMENT;
     std::lock_guard<std::mutex> lk(ex->mu);
     cudaSetDevice(ex->device);
+    ex->check_epoch();
     BatchRun br;
     KunStatus rs = batch_setup(ex, (const KunGpuModuleDesc *)mod, njobs, (const NameMap *const *)buffers,
                                num_stocks, total_time, cur_time, length, br);
@@ -287,6 +287,7 @@ KUN_EXPORT int kunExecutorTune(KunExecutorHandle exec, KunModuleHandle mod, int 
     if (!ex) return -1;
     std::lock_guard<std::mutex> lk(ex->mu);
     cudaSetDevice(ex->device);
+    ex->check_epoch();
     const auto *m = (const KunGpuModuleDesc *)mod;
     BatchRun br;
     if (batch_setup(ex, m, njobs, (const NameMap *const *)buffers, num_stocks, total_time, cur_time, length, br) !=

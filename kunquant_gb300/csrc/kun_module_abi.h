@@ -11,7 +11,7 @@
 extern "C" {
 #endif
 
-#define KUN_GPU_MODULE_ABI 0x6b470007ull
+#define KUN_GPU_MODULE_ABI 0x6b470008ull
 #define KUN_BLOCK_REGCAP 0x10000
 
 typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
@@ -41,7 +41,6 @@ typedef struct {
     int64_t length;
     const int32_t *ring_pos;   /* unused */
     void *state;               /* stream mode: the stage's float/double state arrays */
-    int32_t *error_flag;       /* device word; kernels set it instead of trapping */
     /* stream mode: stocks live in rings of num_stocks (capacity) columns; a
      * launch covers `nseg` segments (sessions): segment k holds stocks
      * [seg_stock0[k], seg_stock0[k] + seg_off[k+1] - seg_off[k]) and is at
@@ -93,6 +92,11 @@ typedef struct {
     int32_t state_t_vars;      /* float/double arrays of num_stocks */
     int32_t state_i_vars;      /* int32 arrays of num_stocks */
     KunGpuLaunchFn init;
+    /* per int32 state array: the largest value a restored state may hold
+     * (valid values are 0..max), or -1 where any value is safe (tick
+     * indices); the runtime checks restored dumps against it before any
+     * kernel reads them.  NULL when state_i_vars is 0. */
+    const int32_t *state_i_max;
     /* time-series stages with grouped launches: per kernel, default time
      * tile << 1 (or number of scan roles << 1) | 1 for a scan kernel */
     const int32_t *kernel_info;

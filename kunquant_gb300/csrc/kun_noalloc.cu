@@ -27,18 +27,24 @@
 
 namespace kungpu {
 
-// Bytes 0..255 hold the device error word passed to the kernels; the
-// temporaries and scratch slots follow.
+// The temporaries and scratch slots of one run, slot after slot.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[KUN_NOALLOC_SCRATCH_BYTES];
 
-static constexpr size_t kHeader = 256;
 static constexpr int kMaxDevices = 64;
+
+// A cached plan, with the descriptor fields it was made from: a plan is
+// reused only for the same module contents, and every plan is dropped when
+// a library is unloaded (another one can then load at the same address).
+struct CachedPlan {
+    Plan plan;
+    int num_buffers, num_stages, dtype;
+    const void *stages, *buffers;
+};
 
 static std::mutex g_mu;
 static void *g_base[kMaxDevices];
-static std::map<std::tuple<const void *, long long, long long>, Plan> g_plans;
-
-static size_t round_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+static std::map<std::tuple<const void *, long long, long long>, CachedPlan> g_plans;
+static uint64_t g_plans_epoch = 0;
 
 static bool on_device(const void *p) {
     cudaPointerAttributes a;
@@ -92,15 +98,31 @@ static KunStatus no_alloc_run(const KunGpuModuleDesc *m, const NameMap &names, l
         g_base[dev] = p;
     }
     char *base = (char *)g_base[dev];
+    if (g_plans_epoch != library_epoch()) {
+        g_plans.clear();
+        g_plans_epoch = library_epoch();
+    }
     auto key = std::make_tuple((const void *)m, S, length);
     auto it = g_plans.find(key);
-    if (it == g_plans.end()) {
-        Plan p;
-        if (!make_plan(m, S, length, 1, p)) return KUN_INVALID_ARGUMENT;
-        it = g_plans.emplace(key, std::move(p)).first;
+    if (it != g_plans.end() &&
+        (it->second.num_buffers != m->num_buffers || it->second.num_stages != m->num_stages ||
+         it->second.dtype != m->dtype || it->second.stages != (const void *)m->stages ||
+         it->second.buffers != (const void *)m->buffers)) {
+        g_plans.erase(it);
+        it = g_plans.end();
     }
-    const Plan &plan = it->second;
-    size_t need = kHeader + plan.slot_bytes * (size_t)plan.num_slots;
+    if (it == g_plans.end()) {
+        CachedPlan c;
+        if (!make_plan(m, S, length, 1, c.plan)) return KUN_INVALID_ARGUMENT;
+        c.num_buffers = m->num_buffers;
+        c.num_stages = m->num_stages;
+        c.dtype = m->dtype;
+        c.stages = m->stages;
+        c.buffers = m->buffers;
+        it = g_plans.emplace(key, std::move(c)).first;
+    }
+    const Plan &plan = it->second.plan;
+    size_t need = plan.slot_bytes * (size_t)plan.num_slots;
     if (need > (size_t)KUN_NOALLOC_SCRATCH_BYTES) {
         set_error("kunRunGraphNoAlloc: module %s with %lld stocks x %lld time steps needs %zu bytes of scratch "
                   "(%d slots of %zu bytes); the static scratch holds %zu bytes. Use kunRunGraphEx, or fewer "
@@ -112,7 +134,7 @@ static KunStatus no_alloc_run(const KunGpuModuleDesc *m, const NameMap &names, l
     for (int b = 0; b < m->num_buffers; b++) {
         const KunGpuBufferDesc &bd = m->buffers[b];
         if (bd.kind == KUN_BUF_TEMP) {
-            if (plan.temp_slot[b] >= 0) ptrs[b] = base + kHeader + plan.slot_bytes * (size_t)plan.temp_slot[b];
+            if (plan.temp_slot[b] >= 0) ptrs[b] = base + plan.slot_bytes * (size_t)plan.temp_slot[b];
             continue;
         }
         auto f = names.find(bd.name);
@@ -126,19 +148,14 @@ static KunStatus no_alloc_run(const KunGpuModuleDesc *m, const NameMap &names, l
         }
         ptrs[b] = f->second;
     }
-    // Only the error word must start at zero: every temporary and scratch
-    // slot is written by its producer before any kernel reads it.
-    int32_t *err = (int32_t *)base;
-    cudaError_t e = cudaMemsetAsync(err, 0, sizeof(int32_t), st);
-    if (e != cudaSuccess) {
-        set_error("kunRunGraphNoAlloc: %s", cudaGetErrorString(e));
-        return KUN_CUDA_ERROR;
-    }
+    // Nothing has to start at zero: every temporary and scratch slot is
+    // written by its producer before any kernel reads it, so the contents a
+    // previous call left behind are never seen.
     std::vector<void *> scratch;
     for (int si : plan.order) {
         const KunGpuStageDesc &s = m->stages[si];
         scratch.clear();
-        for (int sl : plan.scratch[si]) scratch.push_back(base + kHeader + plan.slot_bytes * (size_t)sl);
+        for (int sl : plan.scratch[si]) scratch.push_back(base + plan.slot_bytes * (size_t)sl);
         KunGpuStageArgs a;
         memset(&a, 0, sizeof a);
         a.buffers = ptrs.data();
@@ -147,7 +164,6 @@ static KunStatus no_alloc_run(const KunGpuModuleDesc *m, const NameMap &names, l
         a.total_time = total_time;
         a.start = cur_time;
         a.length = length;
-        a.error_flag = err;
         int rc = s.launch(&a, (void *)st);
         if (rc != 0) {
             set_error("stage %d (%s) launch failed: %s", si, s.name, cudaGetErrorString((cudaError_t)rc));

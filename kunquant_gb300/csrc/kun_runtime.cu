@@ -7,6 +7,8 @@
 // Runtime.cpp:84-93), and the stage kernels are enqueued on the executor's
 // CUDA stream.  Host buffers are staged to the device inside the call.
 #include <cuda_runtime.h>
+
+#include <atomic>
 #include <dlfcn.h>
 
 #include <algorithm>
@@ -260,7 +262,6 @@ static KunStatus enqueue_stages(Executor *ex, const KunGpuModuleDesc *m, const P
         a.total_time = total_time;
         a.start = cur_time;
         a.length = length;
-        a.error_flag = ex->d_error;
         auto tn = ex->tuning.find((const void *)m);
         if (tn != ex->tuning.end() && si < (int)tn->second.size() && !tn->second[si].tile.empty()) {
             a.tune_tile = tn->second[si].tile.data();
@@ -283,6 +284,21 @@ static KunStatus enqueue_stages(Executor *ex, const KunGpuModuleDesc *m, const P
         for (int k = 1; k < plan.num_streams; k++)
             if (last_on[k] >= 0) cudaStreamWaitEvent(origin, ex->done[last_on[k]], 0);
     return KUN_SUCCESS;
+}
+
+static std::atomic<uint64_t> g_library_epoch{0};
+uint64_t library_epoch() { return g_library_epoch.load(); }
+
+void Executor::check_epoch() {
+    uint64_t e = library_epoch();
+    if (e == epoch) return;
+    for (auto &s : streams) cudaStreamSynchronize(s);
+    for (auto &g : graphs) cudaGraphExecDestroy(g.exec);
+    graphs.clear();
+    seen.clear();
+    plans.clear();
+    tuning.clear();
+    epoch = e;
 }
 
 KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &names, long long S,
@@ -313,6 +329,7 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
     }
     std::lock_guard<std::mutex> lk(ex->mu);
     cudaSetDevice(ex->device);
+    ex->check_epoch();
     bool multi = ex->streams.size() > 1 && !ex->profile;
     int nstreams = multi ? (int)ex->streams.size() : 1;
     auto key = std::make_tuple((const void *)m, S, length, nstreams);
@@ -505,8 +522,7 @@ Executor *create_executor(int nstreams) {
         }
         ex->streams.push_back(s);
     }
-    if (cudaMalloc(&ex->d_error, sizeof(int32_t)) == cudaSuccess) cudaMemset(ex->d_error, 0, sizeof(int32_t));
-    else cudaGetLastError();
+    ex->epoch = library_epoch();
     return ex;
 }
 
@@ -522,7 +538,6 @@ void destroy_executor(Executor *ex) {
     if (ex->fork) cudaEventDestroy(ex->fork);
     if (ex->bridge_in) cudaEventDestroy(ex->bridge_in);
     if (ex->bridge_out) cudaEventDestroy(ex->bridge_out);
-    if (ex->d_error) cudaFree(ex->d_error);
     for (auto cs : ex->copy_streams) {
         cudaStreamSynchronize(cs);
         cudaStreamDestroy(cs);
@@ -577,6 +592,7 @@ KUN_EXPORT void kunUnloadLibrary(KunLibraryHandle ptr) {
     if (!lib) return;
     if (lib->handle) dlclose(lib->handle);
     delete lib;
+    g_library_epoch.fetch_add(1);
 }
 
 KUN_EXPORT KunBufferNameMapHandle kunCreateBufferNameMap(void) { return new NameMap(); }

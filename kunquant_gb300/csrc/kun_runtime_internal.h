@@ -62,6 +62,11 @@ struct Plan {
     size_t slot_bytes = 0;
 };
 
+// Number of kunUnloadLibrary calls so far.  Caches keyed by a module
+// descriptor's address (plans, captured graphs, tuned shapes) are dropped
+// when it changes: another library can be loaded at the same address.
+uint64_t library_epoch();
+
 // Builds the stage order and the slot assignment of temporaries and scratch
 // for `nstreams` streams; false (with the error set) on a cyclic stage graph.
 bool make_plan(const KunGpuModuleDesc *m, long long S, long long length, int nstreams, Plan &p);
@@ -80,8 +85,8 @@ struct Executor {
     cudaStream_t user_stream = nullptr;
     Arena arena;
     Arena staging;
-    int32_t *d_error = nullptr;
     int64_t last_launches = 0;
+    uint64_t epoch = 0;  // library_epoch() the module caches below belong to
     std::map<std::tuple<const void *, long long, long long, int>, Plan> plans;
     std::mutex mu;
     // optional per-stage timing (CUDA events around every launch)
@@ -114,6 +119,9 @@ struct Executor {
     std::vector<cudaEvent_t> copy_ev;    // per stage: its outputs are ready
     std::vector<cudaEvent_t> copy_done;  // per copy stream: all copies issued so far are done
     cudaStream_t stream() const { return streams[0]; }
+    // drops plans, graphs and tuned shapes if a library was unloaded since
+    // they were made (call with `mu` held)
+    void check_epoch();
 };
 
 // Device state of a stream module for `cap` stock columns: per buffer a ring

@@ -406,72 +406,107 @@ bool serialize_range(const StreamStore &store, long long col0, long long n, long
     return true;
 }
 
-// Restores a range; on failure sets the reference's error text.
-bool deserialize_range(StreamStore &store, long long col0, long long n, long long &tick, std::vector<int> &last_row,
-                       Reader &r, cudaStream_t st) {
-    const KunGpuModuleDesc *m = store.m;
+// A dump read and checked on the host: every ring and state array of a
+// range of `n` stocks, as laid out in the file.
+struct ParsedDump {
+    long long tick = 0;
+    std::vector<int> last_row;
+    std::vector<std::vector<char>> rings;         // per buffer [window][n]
+    std::vector<std::vector<char>> st_t, st_i;    // per stage [vars][n]
+};
+
+// Reads a dump for `n` stocks of module `m` and checks every value a kernel
+// would use as an index or a loop bound: ring rows in [0, window), the tick
+// non-negative, and each int32 state within the bounds the module declares
+// (state_i_max).  Touches no device memory; on failure sets the reference's
+// error text (cpp/Kun/Runtime.cpp:418,456).
+static bool parse_dump(const KunGpuModuleDesc *m, long long n, Reader &r, ParsedDump &d) {
     size_t elem = elem_of(m);
     char magic[8];
     uint32_t ver, dt, nb, ns;
     int64_t stocks, tk;
     char name[64];
     if (!r.read(magic, 8) || memcmp(magic, kMagic, 8) || !r.read(&ver, 4) || ver != 1 || !r.read(&dt, 4) ||
-        dt != (uint32_t)m->dtype || !r.read(&stocks, 8) || stocks != n || !r.read(&tk, 8) || !r.read(&nb, 4) ||
-        nb != (uint32_t)m->num_buffers || !r.read(&ns, 4) || ns != (uint32_t)m->num_stages || !r.read(name, 64) ||
-        strncmp(name, m->name, 63)) {
+        dt != (uint32_t)m->dtype || !r.read(&stocks, 8) || stocks != n || !r.read(&tk, 8) || tk < 0 ||
+        !r.read(&nb, 4) || nb != (uint32_t)m->num_buffers || !r.read(&ns, 4) || ns != (uint32_t)m->num_stages ||
+        !r.read(name, 64) || strncmp(name, m->name, 63)) {
         set_error("Failed to read initial stream buffer");
         return false;
     }
-    std::vector<char> host;
-    last_row.assign(m->num_buffers, 0);
+    d.tick = tk;
+    d.last_row.assign(m->num_buffers, 0);
+    d.rings.assign(m->num_buffers, {});
     for (int b = 0; b < m->num_buffers; b++) {
         int32_t win, lr;
         if (!r.read(&win, 4) || win != win_of(m, b) || !r.read(&lr, 4) || lr < 0 || lr >= win) {
             set_error("Failed to read initial stream buffer");
             return false;
         }
-        last_row[b] = lr;
-        host.resize((size_t)win * n * elem);
-        if (!r.read(host.data(), host.size())) {
+        d.last_row[b] = lr;
+        d.rings[b].resize((size_t)win * n * elem);
+        if (!r.read(d.rings[b].data(), d.rings[b].size())) {
             set_error("Failed to read initial stream buffer");
             return false;
         }
-        host_to_dev_cols(store.rings[b], host, elem, store.cap, win, col0, n, st);
-        cudaStreamSynchronize(st);
     }
+    d.st_t.assign(m->num_stages, {});
+    d.st_i.assign(m->num_stages, {});
     for (int s = 0; s < m->num_stages; s++) {
-        const KunGpuStageDesc &d = m->stages[s];
+        const KunGpuStageDesc &sd = m->stages[s];
         int32_t nt, ni;
-        if (!r.read(&nt, 4) || nt != d.state_t_vars || !r.read(&ni, 4) || ni != d.state_i_vars) {
+        if (!r.read(&nt, 4) || nt != sd.state_t_vars || !r.read(&ni, 4) || ni != sd.state_i_vars) {
             set_error("Failed to deserialize state buffer");
             return false;
         }
-        if (nt) {
-            host.resize((size_t)nt * n * elem);
-            if (!r.read(host.data(), host.size())) {
-                set_error("Failed to deserialize state buffer");
-                return false;
-            }
-            host_to_dev_cols(store.st_t[s], host, elem, store.cap, nt, col0, n, st);
-            cudaStreamSynchronize(st);
+        d.st_t[s].resize((size_t)nt * n * elem);
+        d.st_i[s].resize((size_t)ni * n * 4);
+        if ((nt && !r.read(d.st_t[s].data(), d.st_t[s].size())) ||
+            (ni && !r.read(d.st_i[s].data(), d.st_i[s].size()))) {
+            set_error("Failed to deserialize state buffer");
+            return false;
         }
-        if (ni) {
-            host.resize((size_t)ni * n * 4);
-            if (!r.read(host.data(), host.size())) {
-                set_error("Failed to deserialize state buffer");
-                return false;
+        if (ni && !sd.state_i_max) {
+            set_error("Failed to deserialize state buffer");
+            return false;
+        }
+        const int32_t *iv = (const int32_t *)d.st_i[s].data();
+        for (int v = 0; v < ni; v++) {
+            const int32_t mx = sd.state_i_max[v];
+            if (mx < 0) continue;
+            for (long long k = 0; k < n; k++) {
+                const int32_t x = iv[(size_t)v * n + k];
+                if (x < 0 || x > mx) {
+                    set_error("Failed to deserialize state buffer");
+                    return false;
+                }
             }
-            host_to_dev_cols(store.st_i[s], host, 4, store.cap, ni, col0, n, st);
-            cudaStreamSynchronize(st);
         }
     }
-    tick = tk;
     return true;
+}
+
+// Copies a checked dump into columns [col0, col0 + n) of the store.
+static bool upload_dump(StreamStore &store, long long col0, long long n, const ParsedDump &d, cudaStream_t st) {
+    const KunGpuModuleDesc *m = store.m;
+    size_t elem = elem_of(m);
+    bool ok = true;
+    for (int b = 0; b < m->num_buffers; b++)
+        ok = ok && host_to_dev_cols(store.rings[b], d.rings[b], elem, store.cap, win_of(m, b), col0, n, st);
+    for (int s = 0; s < m->num_stages; s++) {
+        const KunGpuStageDesc &sd = m->stages[s];
+        if (sd.state_t_vars)
+            ok = ok && host_to_dev_cols(store.st_t[s], d.st_t[s], elem, store.cap, sd.state_t_vars, col0, n, st);
+        if (sd.state_i_vars)
+            ok = ok && host_to_dev_cols(store.st_i[s], d.st_i[s], 4, store.cap, sd.state_i_vars, col0, n, st);
+    }
+    ok = cudaStreamSynchronize(st) == cudaSuccess && ok;
+    if (!ok) set_error("Failed to deserialize state buffer");
+    return ok;
 }
 
 static StreamCtx *create_ctx(Executor *ex, const KunGpuModuleDesc *m, long long S, Reader *init, KunStatus &rc) {
     rc = KUN_INVALID_ARGUMENT;
-    if (!ex || !m) {
+    if (!m) {
         set_error("null executor or module");
         return nullptr;
     }
@@ -485,6 +520,16 @@ static StreamCtx *create_ctx(Executor *ex, const KunGpuModuleDesc *m, long long 
     }
     if (S <= 0) {
         set_error("Bad num_stocks");
+        return nullptr;
+    }
+    // a restored dump is read and checked in full before any device work
+    ParsedDump dump;
+    if (init && !parse_dump(m, S, *init, dump)) {
+        rc = KUN_INIT_ERROR;
+        return nullptr;
+    }
+    if (!ex) {
+        set_error("null executor or module");
         return nullptr;
     }
     cudaSetDevice(ex->device);
@@ -517,7 +562,9 @@ static StreamCtx *create_ctx(Executor *ex, const KunGpuModuleDesc *m, long long 
     c->last_row.resize(m->num_buffers);
     for (int b = 0; b < m->num_buffers; b++) c->last_row[b] = win_of(m, b) - 1;
     if (init) {
-        if (!deserialize_range(c->store, 0, S, c->tick, c->last_row, *init, st)) {
+        c->tick = dump.tick;
+        c->last_row = dump.last_row;
+        if (!upload_dump(c->store, 0, S, dump, st)) {
             rc = KUN_INIT_ERROR;
             delete c;
             return nullptr;

@@ -22,7 +22,11 @@ def _front_end():
     try:
         import KunQuant.Op  # noqa: F401
     except ImportError:
-        root = os.environ.get("KUN_REFERENCE_ROOT", "/root/reference")
+        # the reference checkout, by default the "reference" folder beside
+        # this repository
+        repo = os.path.dirname(os.path.dirname(HERE))
+        root = os.environ.get("KUN_REFERENCE_ROOT",
+                              os.path.join(os.path.dirname(repo), "reference"))
         sys.path.append(root)
         import KunQuant.Op  # noqa: F401
 

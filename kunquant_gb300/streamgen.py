@@ -43,6 +43,7 @@ class StreamGen(StageGen):
         self.fplan = contraction.plan(self.ops) if self.st["kind"] == "ts" else {}
         self.state_t_vars = 0
         self.state_i_vars = 0
+        self.state_i_max: List[int] = []
         self.has_init = False
         self.windows = {b["id"]: b["window"] for b in spec["buffers"]}
 
@@ -143,6 +144,12 @@ class StreamGen(StageGen):
             nt += len(tf)
             ni += len(inf)
         self.state_t_vars, self.state_i_vars = nt, ni
+        # bounds a restored int state must respect: NaN counts, window sizes
+        # and insert ranks lie in [0, window]; tick indices are free
+        self.state_i_max = []
+        for i, (tf, inf) in fields.items():
+            W = int(ops[i].get("window", 0))
+            self.state_i_max += [-1 if f.startswith(("ix[", "idx[")) else W for f in inf]
         self.has_init = bool(fields)
         # rings of the buffers the stage touches
         decl = []

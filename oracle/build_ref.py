@@ -31,8 +31,11 @@ import sys
 import sysconfig
 from concurrent.futures import ThreadPoolExecutor
 
-REF_ROOT = os.environ.get("KUN_REFERENCE_ROOT", "/root/reference")
 HERE = os.path.dirname(os.path.abspath(__file__))
+# the reference checkout: $KUN_REFERENCE_ROOT, by default the "reference"
+# folder beside this repository
+REF_ROOT = os.environ.get("KUN_REFERENCE_ROOT",
+                          os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 OUT = os.path.join(HERE, "_ref")
 PYROOT = os.path.join(OUT, "py")
 RUNNER_DIR = os.path.join(PYROOT, "KunQuant", "runner")

@@ -3,7 +3,7 @@ on the predefined graphs -- TEST INFRASTRUCTURE, this container only.
 
 Used to pin the oracle restatement and to generate the golden fixtures under
 ``tests/golden``.  Needs the reference sources (``$KUN_REFERENCE_ROOT``,
-default ``/root/reference``); it is never imported on the product path and
+default the ``reference`` folder beside this repository); it is never imported on the product path and
 never on the GPU machine.
 """
 import dataclasses

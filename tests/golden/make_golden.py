@@ -1,6 +1,7 @@
 """Generates the golden fixtures of tests/golden from the reference itself.
 
-Needs the reference sources (``$KUN_REFERENCE_ROOT``, default /root/reference):
+Needs the reference sources (``$KUN_REFERENCE_ROOT``, default the
+``reference`` folder beside this repository):
 the reference CPU runtime is built by ``oracle/build_ref.py`` and its own JIT
 compiles every graph below.  For each case the fixture holds the inputs, the
 reference's outputs and the module spec the GPU backend compiles, so the tests

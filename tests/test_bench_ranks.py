@@ -55,6 +55,22 @@ def test_reference_arm_prints_from_rank0_only(tmp_path):
     assert d["e2e"]["h2d_bytes_per_step"] == 0
 
 
+def test_gpus_flag_launches_the_replicas_itself():
+    """`bench.py --gpus 2` with no launcher starts two ranks by itself; the
+    single line comes from rank 0 and counts both."""
+    env = {k: v for k, v in os.environ.items() if k not in ("WORLD_SIZE", "RANK", "LOCAL_RANK")}
+    env["CUDA_VISIBLE_DEVICES"] = ""
+    cmd = [sys.executable, "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0",
+           "--stocks", "200", "--days", "120"]
+    r = subprocess.run(cmd, cwd=REPO, env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    d = json.loads(lines[0])
+    # n_gpus is the launched world size, read by the rank from WORLD_SIZE
+    assert d["impl"] == "reference" and d["n_gpus"] == 2
+
+
 def test_factor_errors_matches_numpy():
     """The GPU precision report's error measure, run on CPU tensors, equals
     the numpy form of the same definition."""

@@ -38,36 +38,56 @@ def test_no_alloc_source_allocates_nothing():
     assert "cudaGetSymbolAddress" in code
 
 
-@pytest.mark.gpu
-def test_no_alloc_matches_run_graph_twice():
+def _check_twice(key, module, S, T, cur_time, seed):
+    """Two no-alloc calls in a row on fresh output buffers, each equal bit
+    for bit to kunRunGraphEx; the second call changes no device memory."""
     import torch
-    S, T = 128, 200
-    mod = kr.Library.predefined("alpha158_f32").getModule("alpha158")
-    data = synth.ohlcv(S, T, seed=7, nan_frac=0.005)
+    mod = kr.Library.predefined(key).getModule(module)
+    data = synth.ohlcv(S, T, seed=seed, nan_frac=0.005)
     dev_in = {k: torch.from_numpy(v).cuda() for k, v in data.items() if k in mod.getInputNames()}
     L, run_no_alloc = _no_alloc_fn()
+    length = T - cur_time
 
     # existing entry point, device buffers, own executor
     ex = kr.createSingleThreadExecutor()
-    want = kr.runGraph(ex, mod, dev_in, 0, T)
+    want = kr.runGraph(ex, mod, dev_in, cur_time, length)
     torch.cuda.synchronize()
     want = {k: v.cpu().numpy() for k, v in want.items()}
 
     stream = torch.cuda.current_stream()
     for call in range(2):
-        outs = {k: torch.full((T, S), float("nan"), device="cuda") for k in mod.getOutputNames()}
+        outs = {k: torch.full((length, S), float("nan"), device="cuda") for k in mod.getOutputNames()}
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         m = L.kunCreateBufferNameMap()
         try:
             for k, v in list(dev_in.items()) + list(outs.items()):
                 L.kunSetBufferNameMap(m, k.encode(), ctypes.c_void_p(v.data_ptr()))
-            rc = run_no_alloc(mod.handle, m, S, T, 0, T, ctypes.c_void_p(stream.cuda_stream))
+            rc = run_no_alloc(mod.handle, m, S, T, cur_time, length, ctypes.c_void_p(stream.cuda_stream))
         finally:
             L.kunDestoryBufferNameMap(m)
         assert rc == 0, L.kunGetLastError().decode()
         stream.synchronize()
+        free_after = torch.cuda.mem_get_info()[0]
+        if call == 1:
+            # the first call may load the module's kernels; the second finds
+            # everything in place and takes no device memory
+            assert free_after == free_before, (free_before, free_after)
         got = {k: v.cpu().numpy() for k, v in outs.items()}
         bad = compare_exact(got, want)
-        assert not bad, f"call {call}: differs from kunRunGraphEx: {bad}"
+        assert not bad, f"{key} call {call}: differs from kunRunGraphEx: {bad}"
+
+
+@pytest.mark.gpu
+def test_no_alloc_matches_run_graph_twice():
+    _check_twice("alpha158_f32", "alpha158", 128, 200, 0, seed=7)
+
+
+@pytest.mark.gpu
+def test_no_alloc_alpha101_rank_and_scratch_with_offset():
+    # Alpha101: cross-sectional Rank/Scale stages, per-stage scratch slots and
+    # a run that starts at cur_time > 0
+    _check_twice("alpha101_f32", "alpha101", 96, 260, 50, seed=8)
 
 
 @pytest.mark.gpu
