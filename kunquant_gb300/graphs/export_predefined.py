@@ -68,6 +68,10 @@ CONFIGS = {
     "alpha101_f32": (build_alpha101, "alpha101", dict(
         dtype="float", input_layout="TS", output_layout="TS",
         options={"opt_reduce": True, "fast_log": True})),
+    # the reference's default layout in and out: [S/8][T][8]
+    "alpha101_sts_f32": (build_alpha101, "alpha101_sts", dict(
+        dtype="float", input_layout="STs", output_layout="STs",
+        options={"opt_reduce": True, "fast_log": True})),
     "alpha101_f64": (build_alpha101, "alpha101_f64", dict(
         dtype="double", input_layout="TS", output_layout="TS",
         options={"opt_reduce": True, "fast_log": True, "no_fast_stat": True})),

@@ -236,6 +236,42 @@ def _save(name, spec, inputs, outputs, extra=None):
     print(name, "->", os.path.relpath(path, REPO), os.path.getsize(path), "bytes")
 
 
+def _digest(a) -> str:
+    """SHA-256 of an output's bytes with every NaN written as the one quiet
+    NaN (NaN payloads are not part of the parity contract)."""
+    import hashlib
+    a = np.array(a, copy=True)
+    a[np.isnan(a)] = np.nan
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _save_digests(name, key, inputs, ref, cur_time=0):
+    """A large batch fixture: every reference output as a SHA-256 of its
+    bytes; outputs where the oracle is not bit-identical to the reference are
+    stored in full (the tests hold those to 1e-5)."""
+    from oracle.oracle import OracleProgram
+    from kunquant_gb300.graph import predefined_spec
+    a0 = next(iter(inputs.values()))
+    T = a0.shape[1] if a0.ndim == 3 else a0.shape[0]
+    mine = OracleProgram(predefined_spec(key)).run(inputs, cur_time=cur_time, length=T - cur_time)
+    full = {k: v for k, v in ref.items() if _digest(mine[k]) != _digest(v)}
+    _save(name, {"predefined": key}, inputs, full,
+          {"cur_time": cur_time, "digests": {k: _digest(v) for k, v in ref.items()}})
+
+
+def _stream_ticks(T, dense_from, every):
+    """Ticks whose outputs a stream fixture stores: every `every`-th tick,
+    and every tick from `dense_from` on (past the longest window)."""
+    return [t for t in range(T) if t % every == 0 or t >= dense_from]
+
+
+STREAM_CASES = {
+    # fixture: (library key, stocks, ticks, nan fraction, dense from, every)
+    "alpha101_stream_f32": ("alpha101_stream_f32", 64, 300, 0.0, 240, 8),
+    "alpha158_stream_f32": ("alpha158_stream_f32", 64, 300, 0.002, 240, 8),
+}
+
+
 def predefined_cases():
     from kunquant_gb300 import synth
     from kunquant_gb300.graph import predefined_spec
@@ -295,11 +331,22 @@ def main(names):
         data = synth.ohlcv(S, T, seed=S * 1000 + T, nan_frac=nanf, dtype=dt)
         out = refkun.run_batch(key, data, cur_time=start, length=T - start)
         _save(name, {"predefined": key}, data, out, {"cur_time": start})
-    if not names or "alpha101_stream_f32" in names:
-        key = "alpha101_stream_f32"
-        data = synth.ohlcv(8, 60, seed=99, nan_frac=0.0)
+    if not names or "alpha101_sts_f32" in names:
+        # the reference's own Alpha101 configuration: fp32, STs in and out,
+        # 64 stocks x 260 days
+        S, T = 64, 260
+        data = synth.ohlcv(S, T, seed=S * 1000 + T, nan_frac=0.0)
+        sts = {k: _to_sts(v) for k, v in data.items()}
+        out = refkun.run_batch("alpha101_sts_f32", sts)
+        _save_digests("alpha101_sts_f32", "alpha101_sts_f32", sts, out)
+    for name, (key, S, T, nanf, dense, every) in STREAM_CASES.items():
+        if names and name not in names:
+            continue
+        data = synth.ohlcv(S, T, seed=99 + S + T, nan_frac=nanf)
         out = refkun.run_stream(key, data)
-        _save("alpha101_stream_f32", {"predefined": key}, data, out, {"stream": True})
+        ticks = _stream_ticks(T, dense, every)
+        _save(name, {"predefined": key}, data, {k: v[ticks] for k, v in out.items()},
+              {"stream": True, "ticks": ticks})
     if not names or any(n.startswith("util_") for n in names):
         _utilities()
     for name, (build, cfg, kind) in _graphs().items():

@@ -26,6 +26,15 @@ def load(name):
     return spec, inputs, outputs, meta
 
 
+def digest(a) -> str:
+    """SHA-256 of an output's bytes with every NaN written as the one quiet
+    NaN; large fixtures store reference outputs this way (meta["digests"])."""
+    import hashlib
+    a = np.array(a, copy=True)
+    a[np.isnan(a)] = np.nan
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
 def is_stream(name):
     """Stream-mode fixtures hold the reference StreamContext's outputs."""
     with gzip.open(os.path.join(GOLDEN, name + ".json.gz"), "rb") as f:

@@ -2,15 +2,14 @@
 against the oracle.  The GPU path must be bit-identical to the oracle on every
 output; against the reference the oracle's few known-inexact outputs are held
 to 1e-5."""
-import numpy as np
 import pytest
 
 from kunquant_gb300 import build
 from kunquant_gb300 import runner as kr
 from oracle.oracle import OracleProgram
 from tests import golden_util as G
-from tests.parity import compare_close, compare_exact
-from tests.test_oracle_golden import BATCH, known_inexact, rank_amplified
+from tests.parity import compare_exact
+from tests.test_oracle_golden import BATCH, check_against_reference
 
 _lib = {}
 
@@ -25,7 +24,8 @@ def _module(spec):
         _lib["unit"] = kr.Library.load(build.build_module_library(specs, "kun_golden_units"))
     name = spec["name"]
     if name.startswith(("alpha101", "alpha158")):
-        key = {"alpha101": "alpha101_f32", "alpha158": "alpha158_f32", "alpha101_f64": "alpha101_f64",
+        key = {"alpha101": "alpha101_f32", "alpha101_sts": "alpha101_sts_f32",
+               "alpha158": "alpha158_f32", "alpha101_f64": "alpha101_f64",
                "alpha158_f64": "alpha158_f64", "alpha101_fast": "alpha101_fast_f32",
                "alpha158_fast": "alpha158_fast_f32"}[name]
         if key not in _lib:
@@ -45,10 +45,4 @@ def test_gpu_matches_reference_and_oracle(name):
     want = OracleProgram(spec).run(inp, cur_time=start, length=T - start)
     bad = compare_exact(got, want)
     assert not bad, f"GPU differs from the oracle: {bad}"
-    bad = compare_exact(got, ref)
-    allowed = known_inexact(name)
-    assert set(bad) <= allowed, f"GPU differs from the reference: {sorted(set(bad) - allowed)}"
-    amp = rank_amplified(name)
-    assert not compare_close(got, ref, 1e-5, 1e-6, [k for k in ref if k not in amp])
-    for k in amp:
-        np.testing.assert_array_equal(np.isnan(got[k]), np.isnan(ref[k]))
+    check_against_reference(name, got, ref, meta)

@@ -93,6 +93,18 @@ def test_alpha158_precision_vs_fp64():
     comp = stats["alpha158_comp"]
     assert all(comp[f][1] <= 1e-5 for f in names), [f for f in names if comp[f][1] > 1e-5]
     assert sum(comp[f][2] for f in names) == 0
+    # maximum error: with fp64 or two-float running sums every factor is
+    # within 1e-5 of fp64 everywhere, except those whose loss is in the fp32
+    # factor arithmetic around the sums (the deviations from a window mean
+    # in CORR/CORD, the difference of two sums in VSUMD, the ratio in WVMA
+    # at short windows); for them the two forms agree with each other
+    ill = [f for f in names if f.startswith(("CORR", "CORD", "VSUMD")) or f in ("WVMA5", "WVMA10")]
+    for form in ("alpha158_acc64", "alpha158_comp"):
+        over = [f for f in names if stats[form][f][0] > 1e-5]
+        assert set(over) <= set(ill), (form, sorted(set(over) - set(ill)))
+    for f in ill:
+        a, c = acc[f][0], comp[f][0]
+        assert c <= 2 * a + 1e-5, (f, c, a)
     # compensating only the rolling states already holds every median
     mixed = stats["alpha158_mixed"]
     assert all(mixed[f][1] <= 1e-5 for f in names), [f for f in names if mixed[f][1] > 1e-5]
