@@ -48,7 +48,18 @@ WORKLOADS = {
                            n_inputs=6, n_outputs=158),
     "alpha101_fast": dict(key="alpha101_fast_f32", module="alpha101_fast", stocks=64, days=260, nan=0.0,
                           n_inputs=6, n_outputs=82),
+    # window moments as two-float sliding window sums, scans in time chunks
+    "alpha158_slide": dict(key="alpha158_slide_f32", module="alpha158_slide", stocks=5000, days=2500, nan=0.005,
+                           n_inputs=6, n_outputs=158),
+    "alpha101_slide": dict(key="alpha101_slide_f32", module="alpha101_slide", stocks=64, days=260, nan=0.0,
+                           n_inputs=6, n_outputs=82),
+    # the reference's own Alpha101 configuration: STs layout in and out
+    "alpha101_sts": dict(key="alpha101_sts_f32", module="alpha101_sts", stocks=64, days=260, nan=0.0,
+                         n_inputs=6, n_outputs=82),
 }
+# forms of the headline graph timed in the same run: the baseline (one
+# launch per op) and the sliding-moment form
+FORMS = {"alpha158": ["alpha158_plain", "alpha158_slide"]}
 
 
 def max_over_ranks(ms: float, dist, device: str) -> float:
@@ -389,8 +400,9 @@ def universes_main(args):
 
 PRECISION_FORMS = {
     "alpha158": ["alpha158_f32", "alpha158_fast_f32", "alpha158_mixed_f32", "alpha158_comp_f32",
-                 "alpha158_acc64_f32"],
-    "alpha101": ["alpha101_f32", "alpha101_mixed_f32", "alpha101_comp_f32", "alpha101_acc64_f32"],
+                 "alpha158_acc64_f32", "alpha158_slide_f32"],
+    "alpha101": ["alpha101_f32", "alpha101_mixed_f32", "alpha101_comp_f32", "alpha101_acc64_f32",
+                 "alpha101_slide_f32"],
 }
 
 
@@ -497,6 +509,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the stream-serving measurement")
     ap.add_argument("--no-tune", action="store_true", help="keep the generated launch shapes (no autotuning)")
+    ap.add_argument("--no-forms", action="store_true", help="skip timing the plain and slide forms")
     ap.add_argument("--universes", type=int, default=48, help="universes of the 'universes' workload")
     ap.add_argument("--streams", type=int, default=8, help="CUDA streams for concurrent stages")
     args = ap.parse_args()
@@ -636,6 +649,39 @@ def main():
                           f"{100 * avg[top] / sum(avg.values()):.1f}% of kernel time, single-stream profiled pass)",
                 "whole_step_frac": (wl["n_inputs"] + wl["n_outputs"]) * S * T * elem / (ms_step / 1e3) / 1e9 / peak}
 
+    # the other forms of the same graph on the same inputs and executor
+    forms = None
+    if not args.no_forms and args.workload in FORMS:
+        forms = {}
+        for fw in FORMS[args.workload]:
+            fk = WORKLOADS[fw]
+            fmod = kr.Library.predefined(fk["key"]).getModule(fk["module"])
+            ftuned = 0 if args.no_tune else kr.tune(ex, fmod, [dev_in], reps=2)
+
+            def fstep():
+                kr.runGraph(ex, fmod, dev_in, 0, T, outputs=dev_out)
+
+            for _ in range(args.warmup):
+                fstep()
+            torch.cuda.synchronize()
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            f0.record(stream)
+            flaunch = 0
+            for _ in range(args.steps):
+                fstep()
+                flaunch += ex.last_launch_count()
+            f1.record(stream)
+            torch.cuda.synchronize()
+            fms = max_over_ranks(f0.elapsed_time(f1) / args.steps, dist, "cuda")
+            forms[fw] = {"ms_per_step": fms, "value": job_value(world, S, T, fms), "autotuned_stages": ftuned,
+                         "gpu_launches": flaunch}
+        if "alpha158_plain" in forms:
+            for fw in forms:
+                forms[fw]["over_plain"] = forms["alpha158_plain"]["ms_per_step"] / forms[fw]["ms_per_step"]
+            forms["alpha158"] = {"ms_per_step": ms_step, "value": value,
+                                 "over_plain": forms["alpha158_plain"]["ms_per_step"] / ms_step}
+
     # end to end through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e:
@@ -662,7 +708,7 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": config, "roofline": roofline, "cpu_baseline": cpu,
-                "serving": serve_line,
+                "serving": serve_line, "forms": forms,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
                 "stage_ms": {str(k): round(v, 4) for k, v in sorted(avg.items(), key=lambda x: -x[1])[:8]}}
         print(json.dumps(line))

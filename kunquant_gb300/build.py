@@ -30,11 +30,11 @@ COMMON_FLAGS = ["-gencode", f"arch=compute_{ARCH},code=sm_{ARCH}", "-O3", "-line
 # call kfma() explicitly (see contraction.py)
 MODULE_FLAGS = COMMON_FLAGS + ["-fmad=false"]
 
-# built by build_all(); the other forms (alpha158_fast_f32, alpha101_fast_f32,
-# alpha158_comp_f32, alpha158_acc64_f32, alpha158_plain_f32) are built on
-# first use by predefined_library()
+# built by build_all() (the bench times the slide and plain forms beside the
+# headline); the other forms (the fast-stat, compensated, fp64-sum and STs
+# builds, alpha101_slide_f32) are built on first use by predefined_library()
 PREDEFINED = ["alpha101_f32", "alpha158_f32", "alpha101_f64", "alpha158_f64", "alpha101_stream_f32",
-              "alpha158_stream_f32"]
+              "alpha158_stream_f32", "alpha158_slide_f32", "alpha158_plain_f32"]
 
 
 def _hash(paths: Iterable[str], extra: str) -> str:

@@ -240,6 +240,12 @@ __device__ __forceinline__ DFloat df_add_f(DFloat x, float y) {
     if (!isfinite(s.hi)) return DFloat(s.hi, 0.f);
     return df_fast_two_sum(s.hi, __fadd_rn(s.lo, x.lo));
 }
+// a*b exactly, as a two-float (Dekker's product by one FMA)
+__device__ __forceinline__ DFloat df_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    if (!isfinite(p)) return DFloat(p, 0.f);
+    return DFloat(p, __fmaf_rn(a, b, -p));
+}
 // x + a*b with the product taken exactly (a*b = p + e)
 __device__ __forceinline__ DFloat df_add_prod(DFloat x, float a, float b) {
     const float p = __fmul_rn(a, b);

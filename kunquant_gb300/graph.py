@@ -253,7 +253,14 @@ def predefined_spec(name: str) -> dict:
     keeps the window-loop reductions in Kahan fp32 and makes only the rolling
     states (Kahan window sums, regression sums) two-float compensated.
     ``<base>_plain_f32`` is the one-launch-per-op baseline form of
-    ``<base>_f32``."""
+    ``<base>_f32``.  ``<base>_slide_f32`` is the sliding-moment form
+    (``slide.py``): two-pass window moments expanded into two-float sliding
+    window sums, scans in time chunks."""
+    if name.endswith("_slide_f32"):
+        from . import slide
+        spec = slide.rewrite(predefined_spec(name[:-len("_slide_f32")] + "_f32"))
+        spec["name"] = spec["name"] + "_slide"
+        return spec
     for suffix, sets in (("_acc64_f32", {"accum": "f64"}), ("_comp_f32", {"accum": "df32"}),
                          ("_mixed_f32", {"accum": "df32", "accum_scope": "rolling"}),
                          ("_plain_f32", {"form": "plain"})):

@@ -22,7 +22,10 @@ from typing import Dict, List, Optional, Set, Tuple
 
 from . import contraction
 
-SEQ = {"FastWindowedSum", "WindowedLinearRegression", "ExpMovingAvg"}
+SEQ = {"FastWindowedSum", "WindowedLinearRegression", "ExpMovingAvg", "SlideReduce"}
+# states that depend on the last `window` rows only: a scan over them can
+# start anywhere with a warm-up of one window (time-chunked scans)
+FINITE_SEQ = {"FastWindowedSum", "WindowedLinearRegression", "SlideReduce"}
 UNSUPPORTED: Set[str] = set()
 ACC = {"Accumulator", "SetAccumulator"}
 LR_CONS = {"WindowedLinearRegressionRSqaureImpl", "WindowedLinearRegressionSlopeImpl",
@@ -149,6 +152,8 @@ class StagePlan:
         k = op["k"]
         if k in ("FastWindowedSum", "WindowedLinearRegression", "BackRef"):
             return op["in"][0]
+        if k == "SlideReduce":
+            return op["in"][0]
         if k == "IterValue":
             return op["in"][1]
         if k == "SkipListState":
@@ -163,6 +168,8 @@ class StagePlan:
             ws = self.windowed_source(i)
             if ws is not None and ops[ws]["k"] == "Output":
                 windowed_outputs.add(ws)
+            if op["k"] == "SlideReduce":
+                windowed_outputs |= {j for j in op["in"][:op["nsrc"]] if ops[j]["k"] == "Output"}
         self._windowed_outputs = windowed_outputs
         # ops that do not depend on accumulator values first; then each
         # accumulator group goes to the first scan level after its inputs,
@@ -220,6 +227,12 @@ class StagePlan:
                 lv[i] = _odd_ge(lv[src] + 1 if lv[src] >= 0 else 0)
             elif k == "ExpMovingAvg":
                 lv[i] = _odd_ge(max(lv[j] for j in ins))
+            elif k == "SlideReduce":
+                # window reads of materialised sources, invariants at row t
+                ns = op["nsrc"]
+                base = max([lv[j] + 1 if lv[j] >= 0 else 0 for j in ins[:ns]] +
+                           [self._vl(j) for j in ins[ns:]] + [0])
+                lv[i] = _odd_ge(base)
             elif k in LR_CONS:
                 lv[i] = lv[ins[0]]
                 if any(lv[j] > lv[i] for j in ins[1:]):
@@ -434,6 +447,9 @@ class StagePlan:
             elif k in ("FastWindowedSum", "WindowedLinearRegression"):
                 wreads.add(op["in"][0])
                 deps = [op["in"][0]]
+            elif k == "SlideReduce":
+                wreads |= set(op["in"][:op["nsrc"]])
+                deps = list(op["in"])
             elif k == "Accumulator":
                 deps = []  # its input only orders it; the value is the state
             elif k == "SkipListState":
@@ -461,6 +477,8 @@ VEC_U_ELEM = 2
 VEC_PREFETCH = 0
 VEC_UNROLL = 4
 SCAN_BLOCK = 16
+# window sums (two floats each) one chunked scan of the slide form keeps
+SLIDE_MAX_SUMS = 12
 WIDE_SERIES = 24
 
 
@@ -471,6 +489,11 @@ class LeveledGen(StageGen):
         super().__init__(spec, si, tag)
         self.plan = StagePlan(self.ops, plain=spec.get("form") == "plain")
         self.fplan = contraction.plan(self.ops)
+        # sliding-moment form: running sums as deduplicated two-float window
+        # sums, scans in time chunks (see slide.py)
+        self.slide = spec.get("form") == "slide"
+        self.chunk_mode = False
+        self.mom: Dict[tuple, str] = {}
         self.cur_level = None
         self.cur_comp: Set[int] = set()
         self.vec = False
@@ -512,9 +535,81 @@ class LeveledGen(StageGen):
                     roots = sorted(j for j in mem if ops[j]["k"] in ACC)
                     comp, vr, wr = plan.closure(roots, L)
                     roles.append({"roots": roots, "comp": comp, "vr": vr, "wr": wr})
+                if roles and self.slide:
+                    whole = []
+                    for r in self._slide_roles(roles, L):
+                        if self._chunkable(r):
+                            ks.append({"level": L, "kind": "cscan", "roles": [r]})
+                        else:
+                            whole.append(r)
+                    roles = whole
                 if roles:
                     ks.append({"level": L, "kind": "scan", "roles": roles})
         return ks
+
+    def _chunkable(self, role: dict) -> bool:
+        """A scan role whose states all forget rows older than their window
+        runs in time chunks, each starting one window early."""
+        ops = self.ops
+        return all(ops[i]["k"] in FINITE_SEQ for i in role["comp"] if ops[i]["k"] in SEQ | ACC)
+
+    def _slide_roles(self, roles: List[dict], L: int) -> List[dict]:
+        """Scan roles of the slide form merged when they read a common
+        series through a window: the window sums over the same series share
+        their loads, and sums that several roles need (a mean that is also
+        an invariant of a moment) are kept once.  A merged role holds at most
+        SLIDE_MAX_SUMS window sums (registers)."""
+        ops, plan = self.ops, self.plan
+        items = []
+        rest = []
+        for r in roles:
+            seqs = [i for i in r["roots"] if ops[i]["k"] in FINITE_SEQ]
+            if len(seqs) != 1 or ops[seqs[0]]["k"] == "WindowedLinearRegression":
+                rest.append(r)
+                continue
+            op = ops[seqs[0]]
+            srcs = op["in"][:op["nsrc"]] if op["k"] == "SlideReduce" else op["in"][:1]
+            items.append((set(srcs), op["window"], r))
+        parent = list(range(len(items)))
+
+        def find(x):
+            while parent[x] != x:
+                parent[x] = parent[parent[x]]
+                x = parent[x]
+            return x
+
+        for a in range(len(items)):
+            for b in range(a):
+                if items[a][0] & items[b][0]:
+                    parent[find(a)] = find(b)
+        groups: Dict[int, list] = {}
+        for a in range(len(items)):
+            groups.setdefault(find(a), []).append(items[a])
+        out = []
+        for mem in groups.values():
+            # windows in ascending order; a new part starts when the sums
+            # would exceed the cap
+            mem.sort(key=lambda it: (it[1], sorted(it[0])))
+            part: List[int] = []
+            for srcs, w, r in mem:
+                trial = sorted(set(part) | set(r["roots"]))
+                comp, _, _ = plan.closure(trial, L)
+                self._moment_registry(comp)
+                nsum = sum(1 for k in self.mom if k[0] == "s")
+                if part and nsum > SLIDE_MAX_SUMS:
+                    out.append(part)
+                    part = list(r["roots"])
+                else:
+                    part = trial
+            if part:
+                out.append(part)
+        res = []
+        for roots in out:
+            roots = sorted(set(roots))
+            comp, vr, wr = plan.closure(roots, L)
+            res.append({"roots": roots, "comp": comp, "vr": vr, "wr": wr})
+        self.mom = {}
+        return res + rest
 
     def _weight(self, comp: Set[int]) -> float:
         ops = self.ops
@@ -625,7 +720,16 @@ class LeveledGen(StageGen):
         elif k in REDUCTIONS:
             pass
         elif k == "BackRef":
-            self.lines.append(f"{ind}const {T} v{i} = {self.window_read(a[0], op['window'])};")
+            # in a time chunk a BackRef still reads the real earlier row
+            rd = (StageGen.window_read(self, a[0], op['window']) if self.chunk_mode
+                  else self.window_read(a[0], op['window']))
+            self.lines.append(f"{ind}const {T} v{i} = {rd};")
+        elif k == "FastWindowedSum" and self.slide:
+            w = op["window"]
+            nn, sm = self.mom[("nn", a[0], w)], self.mom[("s", ((a[0], 1),), w)]
+            self.lines.append(f"{ind}const {T} v{i} = ({nn} == 0) ? ({T}){sm} : kun::knan<{T}>();")
+        elif k == "SlideReduce":
+            self.lines.append(f"{ind}const {T} v{i} = {self._slide_value(i)};")
         elif k == "FastWindowedSum":
             self.lines.append(f"{ind}const {T} v{i} = ({T})fw{i}.step({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
         elif k == "WindowedLinearRegression":
@@ -694,6 +798,8 @@ class LeveledGen(StageGen):
     def _state_decl(self, i: int) -> Optional[str]:
         op, T = self.ops[i], self.T
         k = op["k"]
+        if k == "SlideReduce" or (k == "FastWindowedSum" and self.slide):
+            return None  # window sums of the role's moment registry
         if k == "FastWindowedSum":
             return f"kun::FWSum<{self.RT}> fw{i}({op['window']});"
         if k == "Accumulator":
@@ -711,6 +817,107 @@ class LeveledGen(StageGen):
                 return f"kun::RegWindow<{T}, {op['window']}, {idx}> sl{i};"
             return f"kun::SortedWindow<{op['window']}> sl{i};"
         return None
+
+    # ------------------------------------------------------------ moments
+    def _moment_registry(self, comp: Set[int]):
+        """Window sums and NaN counts the role's running sums need, each
+        once: ("nn", series, w) counts the NaN rows of a series in the
+        window; ("s", monomial, w) is the two-float window sum of a monomial
+        (a product of series values of one row) over its rows whose factors
+        are all numbers."""
+        ops = self.ops
+        mom: Dict[tuple, str] = {}
+
+        def need(key):
+            if key not in mom:
+                mom[key] = (f"nn{len(mom)}" if key[0] == "nn" else f"sm{len(mom)}")
+
+        for i in sorted(comp):
+            op = ops[i]
+            if op["k"] == "FastWindowedSum":
+                need(("nn", op["in"][0], op["window"]))
+                need(("s", ((op["in"][0], 1),), op["window"]))
+            elif op["k"] == "SlideReduce":
+                ns, w = op["nsrc"], op["window"]
+                srcs = op["in"][:ns]
+                for x in srcs:
+                    need(("nn", x, w))
+                for _, se, _ in op["terms"]:
+                    mono = self._mono(srcs, se)
+                    if mono:
+                        need(("s", mono, w))
+        self.mom = mom
+
+    @staticmethod
+    def _mono(srcs: List[int], exps: List[int]) -> tuple:
+        d: Dict[int, int] = {}
+        for x, e in zip(srcs, exps):
+            if e:
+                d[x] = d.get(x, 0) + e
+        return tuple(sorted(d.items()))
+
+    def _moment_decls(self, ind: str) -> List[str]:
+        out = []
+        for key, name in self.mom.items():
+            if key[0] == "nn":
+                out.append(f"{ind}int {name} = {key[2]};")
+            else:
+                out.append(f"{ind}kun::DFloat {name};")
+        return out
+
+    def _moment_updates(self, ind: str):
+        """One row of every window sum of the role: the row leaving the
+        window is taken out (when all its factors are numbers), the new row
+        added; products are exact two-float products."""
+        L, T = self.lines, self.T
+        olds: Dict[tuple, str] = {}
+        for key in self.mom:
+            if key[0] == "nn":
+                _, x, w = key
+                o = f"o{x}_{w}"
+                olds[(x, w)] = o
+                L.append(f"{ind}const {T} {o} = {self.window_read(x, w)};")
+        for key, name in self.mom.items():
+            if key[0] == "nn":
+                _, x, w = key
+                L.append(f"{ind}{name} += (int)(v{x} != v{x}) - (int)({olds[(x, w)]} != {olds[(x, w)]});")
+        for key, name in self.mom.items():
+            if key[0] != "s":
+                continue
+            _, mono, w = key
+            for which in ("old", "new"):
+                vals = {x: (olds[(x, w)] if which == "old" else f"v{x}") for x, _ in mono}
+                ok = " && ".join(f"{vals[x]} == {vals[x]}" for x, _ in mono)
+                fac = [vals[x] for x, e in mono for _ in range(e)]
+                sign = "-" if which == "old" else ""
+                if len(fac) == 1:
+                    upd = f"{name} = kun::df_add_f({name}, {sign}{fac[0]});"
+                else:
+                    op = "ksub" if which == "old" else "kadd"
+                    upd = f"{name} = kun::{op}({name}, kun::df_prod({fac[0]}, {fac[1]}));"
+                L.append(f"{ind}if ({ok}) {upd}")
+
+    def _slide_value(self, i: int) -> str:
+        """The expanded window polynomial, evaluated in two-float arithmetic
+        from the window sums and the invariants, rounded once; NaN while a
+        row of the window has a NaN operand."""
+        op, T = self.ops[i], self.T
+        ns, w = op["nsrc"], op["window"]
+        srcs, invs = op["in"][:ns], op["in"][ns:]
+        acc = None
+        for c, se, ie in op["terms"]:
+            mono = self._mono(srcs, se)
+            f = [self.mom[("s", mono, w)] if mono else f"kun::DFloat({float(w)!r}f)"]
+            for x, e in zip(invs, ie):
+                f += [f"kun::DFloat({self.val(x)})"] * e
+            if c != 1:
+                f.append(f"kun::DFloat({float(c)!r}f)")
+            term = f[0]
+            for g in f[1:]:
+                term = f"kun::kmul({term}, {g})"
+            acc = term if acc is None else f"kun::kadd({acc}, {term})"
+        ok = " && ".join(f"{self.mom[('nn', x, w)]} == 0" for x in sorted(set(srcs)))
+        return f"(({ok}) ? ({T})({acc}) : kun::knan<{T}>())"
 
     def _reg_window(self, i: int) -> bool:
         return self.ops[i]["window"] <= REG_WINDOW_MAX
@@ -766,9 +973,14 @@ class LeveledGen(StageGen):
         ops = self.ops
         n = len(role["vr"]) + sum(1 for i in role["comp"]
                                   if ops[i]["k"] in ("FastWindowedSum", "WindowedLinearRegression", "BackRef"))
+        n += sum(ops[i]["nsrc"] for i in role["comp"] if ops[i]["k"] == "SlideReduce")
+        if self.slide:
+            # chunked scans have threads enough to hide memory latency; keep
+            # the registers for the window sums
+            return 8 if n <= 6 else 4
         return SCAN_BLOCK if n <= 6 else (8 if n <= 12 else 4)
 
-    def _scan_prefetch(self, role: dict, B: int, ind: str):
+    def _scan_prefetch(self, role: dict, B: int, ind: str, chunk: bool = False):
         """Scan role body: rows are processed in blocks of B; every series the
         role reads (values at t and fixed-offset windowed reads) is loaded for
         the whole block first, so the B sequential state updates never wait on
@@ -781,8 +993,16 @@ class LeveledGen(StageGen):
         wins = {}
         for i in sorted(comp):
             k = ops[i]["k"]
+            if k == "BackRef" and chunk:
+                continue  # read directly: it sees rows before the chunk's warm-up
             if k in ("FastWindowedSum", "WindowedLinearRegression", "BackRef"):
                 wins[(ops[i]["in"][0], str(ops[i]["window"]))] = f"pw{i}"
+            elif k == "SlideReduce":
+                for x in ops[i]["in"][:ops[i]["nsrc"]]:
+                    wins.setdefault((x, str(ops[i]["window"])), f"pw{i}_{x}")
+        # in a time chunk the scan runs rows [tw, t1) and stores [t0, t1); the
+        # rows a state would take out before tw were never put in: NaN
+        tbeg, tend, wlo = ("tw", "t1", "tw") if chunk else ("0LL", "length", "0")
         # double-buffered: the loads of block tb + B are issued before the
         # state updates of block tb, so memory latency overlaps the scan.
         # Regression roles compute long enough per row to hide the loads
@@ -801,12 +1021,12 @@ class LeveledGen(StageGen):
         def loads(pre: str, base: str, bi: str):
             for j in series:
                 L.append(f"{bi}#pragma unroll")
-                L.append(f"{bi}for (int u = 0; u < {B}; ++u) {pre}v{j}[u] = ({base} + u < length) ? "
+                L.append(f"{bi}for (int u = 0; u < {B}; ++u) {pre}v{j}[u] = ({base} + u < {tend}) ? "
                          f"b{j}[({base} + u) * st{j}] : kun::knan<{T}>();")
             for src, off, name in wnames:
                 L.append(f"{bi}#pragma unroll")
                 L.append(f"{bi}for (int u = 0; u < {B}; ++u) {{ const long long r = {base} + u - {off}; "
-                         f"{pre}{name[1:]}[u] = (r >= 0 && {base} + u < length) ? b{src}[r * st{src}] : "
+                         f"{pre}{name[1:]}[u] = (r >= {wlo} && {base} + u < {tend}) ? b{src}[r * st{src}] : "
                          f"kun::knan<{T}>(); }}")
 
         if dbl:
@@ -814,8 +1034,8 @@ class LeveledGen(StageGen):
                 L.append(f"{ind}{T} pv{j}[{B}], nv{j}[{B}];")
             for src, off, name in wnames:
                 L.append(f"{ind}{T} {name}[{B}], n{name[1:]}[{B}];")
-            loads("p", "0LL", ind)
-        L.append(f"{ind}for (long long tb = 0; tb < length; tb += {B}) {{")
+            loads("p", tbeg, ind)
+        L.append(f"{ind}for (long long tb = {tbeg}; tb < {tend}; tb += {B}) {{")
         bi = ind + "  "
         if dbl:
             loads("n", f"(tb + {B})", bi)
@@ -829,20 +1049,25 @@ class LeveledGen(StageGen):
         L.append(f"{bi}for (int u = 0; u < {B}; ++u) {{")
         bj = bi + "  "
         L.append(f"{bj}const long long t = tb + u;")
-        L.append(f"{bj}if (t >= length) break;")
+        L.append(f"{bj}if (t >= {tend}) break;")
         for j in sorted(vr):
             if ops[j]["k"] == "Input" and ops[j].get("single_value"):
                 L.append(f"{bj}const {T} v{j} = pv{j};")
             else:
                 L.append(f"{bj}const {T} v{j} = pv{j}[u];")
         self.pf_window = wins
+        self.chunk_mode = chunk
+        if self.slide:
+            self._moment_updates(bj)
         loops = self._loops()
         for i in range(len(ops)):
             if i in comp and ops[i].get("p", -1) < 0:
                 self.emit_top(i, bj, loops, comp)
         self.pf_window = None
+        self.chunk_mode = False
+        guard = "if (t >= t0) " if chunk else ""
         for i in stores:
-            L.append(f"{bj}b{i}[t * st{i}] = {self.val(i)};")
+            L.append(f"{bj}{guard}b{i}[t * st{i}] = {self.val(i)};")
         L.append(f"{bi}}}")
         for j in series if dbl else []:
             L.append(f"{bi}#pragma unroll")
@@ -993,7 +1218,7 @@ class LeveledGen(StageGen):
                 self.scratch[i] = len(self.scratch)
         reads = set()
         for kd in ks:
-            groups = kd["roles"] if kd["kind"] == "scan" else [kd]
+            groups = kd["roles"] if kd["kind"] in ("scan", "cscan") else [kd]
             for g in groups:
                 reads |= g["vr"] | g["wr"]
         mats = sorted(j for j in reads if ops[j]["k"] not in ("Input", "Output", "WindowedTempOutput"))
@@ -1055,6 +1280,27 @@ class LeveledGen(StageGen):
                     self.vec_u = U
                 self.lines.append("  }")
                 kinfo.append((chunk, 0))
+            elif kd["kind"] == "cscan":
+                # one scan role over a time tile of rows, after a warm-up of
+                # its longest window; the tile is a launch parameter like a
+                # time-parallel kernel's
+                r = kd["roles"][0]
+                rr = r["vr"] | r["wr"] | {i for i in r["roots"] if i in self.scratch}
+                for j in sorted(rr):
+                    self._mem_ptr(j, decl, seen)
+                wmax = max(ops[i]["window"] for i in r["comp"] if ops[i]["k"] in FINITE_SEQ)
+                self.lines.append(f"  const long long tile = P.tile[{ki}];")
+                self.lines.append("  const long long t0 = (long long)by * tile;")
+                self.lines.append("  const long long t1 = t0 + tile < length ? t0 + tile : length;")
+                self.lines.append(f"  const long long tw = t0 > {wmax} ? t0 - {wmax} : 0;")
+                for i in sorted(r["comp"]):
+                    sd = self._state_decl(i)
+                    if sd:
+                        self.lines.append(f"  {sd}")
+                self._moment_registry(r["comp"])
+                self.lines += self._moment_decls("  ")
+                self._scan_prefetch(r, self._scan_block(r), "  ", chunk=True)
+                kinfo.append((max(64, (2 * wmax + 15) // 16 * 16), 0))
             else:
                 roles = kd["roles"]
                 self.lines.append("  switch (by) {")
@@ -1074,6 +1320,8 @@ class LeveledGen(StageGen):
                         sd = self._state_decl(i)
                         if sd:
                             self.lines.append(f"    {sd}")
+                    self._moment_registry(r["comp"])
+                    self.lines += self._moment_decls("    ")
                     self._scan_prefetch(r, self._scan_block(r), "    ")
                     self.lines.append("  } break;")
                 self.lines.append("  default: break;")
@@ -1109,7 +1357,8 @@ class LeveledGen(StageGen):
             # time-parallel kernels also come compiled for 64 registers a
             # thread (8 blocks of 128 threads an SM), picked per kernel by the
             # tuner; scan kernels keep one instance
-            for suf, minb in ([("", "KUN_TS_MINB"), ("_r", "8")] if kd["kind"] == "par" else [("", "KUN_TS_MINB")]):
+            for suf, minb in ([("", "KUN_TS_MINB"), ("_r", "8")] if kd["kind"] in ("par", "cscan")
+                              else [("", "KUN_TS_MINB")]):
                 srcs.append(f"""__global__ void __launch_bounds__(KUN_TS_THREADS, {minb}) {kname}{suf}(const {pstruct} P) {{
   const int bx = blockIdx.x, by = blockIdx.y;
 {pick}

@@ -11,7 +11,9 @@ Five fp32 forms run on the GPU over the same seeded inputs:
   * ``alpha158_comp``  -- fp32 factor arithmetic with every running sum
                           (Kahan window sums, window reductions, regression
                           sums) in two-float compensated fp32;
-  * ``alpha158_acc64`` -- the same running sums in fp64 on the GPU.
+  * ``alpha158_acc64`` -- the same running sums in fp64 on the GPU;
+  * ``alpha158_slide`` -- window moments expanded into two-float sliding
+                          window sums, scans in time chunks (slide.py).
 The FP64 oracle (the reference's fp64 TS build restated) is the truth.  For
 each factor the relative error is |got - want| / max(|want|, 1e-3 * m), m the
 factor's median |want| (a floor so that values crossing zero do not divide by
@@ -30,7 +32,7 @@ from oracle.oracle import OracleProgram
 
 FORMS = [("alpha158_f32", "alpha158"), ("alpha158_fast_f32", "alpha158_fast"),
          ("alpha158_mixed_f32", "alpha158_mixed"), ("alpha158_comp_f32", "alpha158_comp"),
-         ("alpha158_acc64_f32", "alpha158_acc64")]
+         ("alpha158_acc64_f32", "alpha158_acc64"), ("alpha158_slide_f32", "alpha158_slide")]
 
 
 def _errors(got, want):
