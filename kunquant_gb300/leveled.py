@@ -976,8 +976,8 @@ class LeveledGen(StageGen):
         n += sum(ops[i]["nsrc"] for i in role["comp"] if ops[i]["k"] == "SlideReduce")
         if self.slide:
             # chunked scans have threads enough to hide memory latency; keep
-            # the registers for the window sums
-            return 8 if n <= 6 else 4
+            # the registers for the window sums (single-buffered)
+            return 4
         return SCAN_BLOCK if n <= 6 else (8 if n <= 12 else 4)
 
     def _scan_prefetch(self, role: dict, B: int, ind: str, chunk: bool = False):
@@ -1008,7 +1008,7 @@ class LeveledGen(StageGen):
         # Regression roles compute long enough per row to hide the loads
         # and keep the registers instead (measured: 478 us single-buffered,
         # 608 us double-buffered at 2000 stocks)
-        dbl = not any(ops[i]["k"] == "WindowedLinearRegression" for i in comp)
+        dbl = not any(ops[i]["k"] == "WindowedLinearRegression" for i in comp) and not self.slide
         series = [j for j in sorted(vr) if not (ops[j]["k"] == "Input" and ops[j].get("single_value"))]
         for j in sorted(vr):
             if j not in series:
