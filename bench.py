@@ -192,9 +192,22 @@ def cpu_reference(workload: dict, steps: int, warmup: int, seconds_target: float
     for _ in range(steps):
         prog.run(data, nthreads=threads)
     dt = (time.perf_counter() - t0) / steps
-    return {"value": S * days / dt, "unit": "stock-days/s", "cores": threads, "kind": "port",
-            "sample": f"{S} stocks x {days} days of the same seeded OHLCV, {steps} timed runs",
-            "s_per_step": dt}
+    out = {"value": S * days / dt, "unit": "stock-days/s", "cores": threads, "kind": "port",
+           "sample": f"{S} stocks x {days} days of the same seeded OHLCV, {steps} timed runs",
+           "s_per_step": dt}
+    # the port's speed against the reference executor itself, measured where
+    # the reference sources are (oracle/port_speed.py)
+    ps = os.path.join(REPO, "profiles", "cpu_port_vs_reference.json")
+    if os.path.exists(ps):
+        with open(ps) as f:
+            rec = json.load(f)
+        base = workload["key"].replace("_slide", "").replace("_plain", "")
+        if base in rec:
+            out["reference_over_port"] = {"value": rec[base]["reference_over_port"],
+                                          "measured": f"{rec['host']}, {rec['threads']} threads, "
+                                                      f"{rec['stocks']} x {rec['days']}",
+                                          "source": "profiles/cpu_port_vs_reference.md"}
+    return out
 
 
 def serving(nsess=256, rate=20000.0, seconds=3.0, warm=250, seed=3):
@@ -550,7 +563,8 @@ def main():
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ref["s_per_step"] * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic", "config": config, "impl": "reference",
-                "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "cpu_baseline": {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample",
+                                                     "reference_over_port") if k in ref},
                 "e2e": {"value": ref["value"], "unit": "stock-days/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
@@ -702,7 +716,7 @@ def main():
     cpu = None
     if rank == 0 and not args.no_cpu:
         ref = cpu_reference(wl, 2, 1, seconds_target=12.0)
-        cpu = {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        cpu = {k: ref[k] for k in ("value", "unit", "cores", "kind", "sample", "reference_over_port") if k in ref}
     if rank == 0:
         line = {"metric": metric, "value": value, "unit": "stock-days/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,

@@ -240,6 +240,43 @@ __device__ __forceinline__ DFloat df_add_f(DFloat x, float y) {
     if (!isfinite(s.hi)) return DFloat(s.hi, 0.f);
     return df_fast_two_sum(s.hi, __fadd_rn(s.lo, x.lo));
 }
+// Running window sums of the sliding-moment form: (hi, lo) with hi the
+// float sum and lo the accumulated rounding errors of its additions (each
+// found exactly by TwoSum), left unnormalised between rows; after n
+// additions the pair holds the exact sum to about n * 2^-48 of the largest
+// partial sum.  The polynomial of the window sums is evaluated the same way.
+__device__ __forceinline__ void df_acc(DFloat &s, float x) {
+    const float h = __fadd_rn(s.hi, x);
+    const float bb = __fsub_rn(h, s.hi);
+    const float err = __fadd_rn(__fsub_rn(s.hi, __fsub_rn(h, bb)), __fsub_rn(x, bb));
+    s.hi = h;
+    s.lo = __fadd_rn(s.lo, err);
+}
+// s += a*b with the product exact (Dekker's product by one FMA)
+__device__ __forceinline__ void df_acc_prod(DFloat &s, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    df_acc(s, p);
+    s.lo = __fadd_rn(s.lo, e);
+}
+// s -= a*b
+__device__ __forceinline__ void df_acc_prod_neg(DFloat &s, float a, float b) {
+    const float p = __fmul_rn(a, b);
+    const float e = __fmaf_rn(a, b, -p);
+    df_acc(s, -p);
+    s.lo = __fsub_rn(s.lo, e);
+}
+// (hi + lo) * b for an unnormalised pair, kept as a pair: hi*b exact plus
+// lo*b rounded
+__device__ __forceinline__ DFloat df_scale(DFloat a, float b) {
+    const float p = __fmul_rn(a.hi, b);
+    return DFloat(p, __fmaf_rn(a.lo, b, __fmaf_rn(a.hi, b, -p)));
+}
+// s += a for pairs (TwoSum of the high parts, low parts added)
+__device__ __forceinline__ void df_acc_pair(DFloat &s, DFloat a) {
+    df_acc(s, a.hi);
+    s.lo = __fadd_rn(s.lo, a.lo);
+}
 // a*b exactly, as a two-float (Dekker's product by one FMA)
 __device__ __forceinline__ DFloat df_prod(float a, float b) {
     const float p = __fmul_rn(a, b);
@@ -435,6 +472,69 @@ template <typename T, int W> struct LinReg {
         T xm = kdiv(xsum, N), ym = kdiv(ysum, N);
         T interp = kfma(-s, xm, ym);
         return ksub(val, kfma(s, T(W), interp));
+    }
+};
+
+// The windowed regression of the sliding-moment form: the same recurrences
+// and NaN rules as LinReg (cpp/Kun/Ops.hpp:377-466), with the index sums
+// (isum, xsum, x2sum: integers below 2^24, exact in float) kept in float and
+// the value sums (ysum, y2sum, xysum) in unnormalised two-float accumulators;
+// the outputs are formed from those sums without the cancellation of fp32.
+template <int W> struct SlideLinReg {
+    float isum = 0, xsum = 0, x2sum = 0;
+    DFloat ysum, y2sum, xysum;
+    int nn = W;
+    template <bool SharedSq>
+    __device__ __forceinline__ void step(float old, float cur) {
+        const float w = (float)W;
+        df_acc_pair(xysum, -ysum);
+        x2sum = __fsub_rn(__fadd_rn(x2sum, isum), __fmul_rn(2.f, xsum));
+        xsum = __fsub_rn(xsum, isum);
+        const bool on = old != old, cn = cur != cur;
+        if (!on) {
+            isum = __fsub_rn(isum, 1.f);
+            df_acc(ysum, -old);
+            df_acc_prod_neg(y2sum, old, old);
+        }
+        nn = nn - (int)on + (int)cn;
+        if (!cn) {
+            isum = __fadd_rn(isum, 1.f);
+            xsum = __fadd_rn(xsum, w);
+            x2sum = __fadd_rn(x2sum, w * w);
+            df_acc(ysum, cur);
+            df_acc_prod(y2sum, cur, cur);
+            df_acc_prod(xysum, w, cur);
+        }
+    }
+    __device__ __forceinline__ float n() const { return (float)(W - nn); }
+    // N*xysum - xsum*ysum, as a normalised pair
+    __device__ __forceinline__ DFloat cov() const {
+        const float N = n();
+        DFloat a = df_scale(xysum, N);
+        df_acc_pair(a, df_scale(ysum, -xsum));
+        return df_fast_two_sum(a.hi, a.lo);
+    }
+    // N*x2sum - xsum*xsum: exact in float
+    __device__ __forceinline__ float varx() const {
+        return __fsub_rn(__fmul_rn(n(), x2sum), __fmul_rn(xsum, xsum));
+    }
+    __device__ __forceinline__ float rsq() const {
+        const float N = n();
+        const DFloat ys = df_fast_two_sum(ysum.hi, ysum.lo);
+        DFloat vy = df_scale(y2sum, N);
+        df_acc_pair(vy, -kmul(ys, ys));
+        const float r = (float)cov();
+        return __fdiv_rn(__fmul_rn(r, r), __fmul_rn(varx(), (float)vy));
+    }
+    __device__ __forceinline__ float slope() const { return __fdiv_rn((float)cov(), varx()); }
+    // val - (slope*W + ym - slope*xm) = (N*val - ysum - slope*(W*N - xsum)) / N
+    __device__ __forceinline__ float resi(float val) const {
+        const float N = n();
+        const float s = slope();
+        DFloat r = df_prod(N, val);
+        df_acc_pair(r, -ysum);
+        df_acc_pair(r, -df_prod(s, __fsub_rn(__fmul_rn((float)W, N), xsum)));
+        return __fdiv_rn((float)r, N);
     }
 };
 

@@ -478,7 +478,9 @@ VEC_PREFETCH = 0
 VEC_UNROLL = 4
 SCAN_BLOCK = 16
 # window sums (two floats each) one chunked scan of the slide form keeps
-SLIDE_MAX_SUMS = 12
+SLIDE_MAX_SUMS = 10
+# rows a chunked scan of the slide form loads at once
+SLIDE_BLOCK = 2
 WIDE_SERIES = 24
 
 
@@ -729,7 +731,8 @@ class LeveledGen(StageGen):
             nn, sm = self.mom[("nn", a[0], w)], self.mom[("s", ((a[0], 1),), w)]
             self.lines.append(f"{ind}const {T} v{i} = ({nn} == 0) ? ({T}){sm} : kun::knan<{T}>();")
         elif k == "SlideReduce":
-            self.lines.append(f"{ind}const {T} v{i} = {self._slide_value(i)};")
+            val = self._slide_value(i, ind)
+            self.lines.append(f"{ind}const {T} v{i} = {val};")
         elif k == "FastWindowedSum":
             self.lines.append(f"{ind}const {T} v{i} = ({T})fw{i}.step({self.window_read(a[0], op['window'])}, {self.val(a[0])});")
         elif k == "WindowedLinearRegression":
@@ -805,6 +808,8 @@ class LeveledGen(StageGen):
         if k == "Accumulator":
             return f"{T} acc{i} = 0;"
         if k == "WindowedLinearRegression":
+            if self.slide:
+                return f"kun::SlideLinReg<{op['window']}> lr{i};"
             return f"kun::LinReg<{self.RT}, {op['window']}> lr{i};"
         if k == "ExpMovingAvg":
             init = f"kun::knan<{T}>()"
@@ -889,35 +894,35 @@ class LeveledGen(StageGen):
                 vals = {x: (olds[(x, w)] if which == "old" else f"v{x}") for x, _ in mono}
                 ok = " && ".join(f"{vals[x]} == {vals[x]}" for x, _ in mono)
                 fac = [vals[x] for x, e in mono for _ in range(e)]
-                sign = "-" if which == "old" else ""
                 if len(fac) == 1:
-                    upd = f"{name} = kun::df_add_f({name}, {sign}{fac[0]});"
+                    upd = f"kun::df_acc({name}, {'-' if which == 'old' else ''}{fac[0]});"
                 else:
-                    op = "ksub" if which == "old" else "kadd"
-                    upd = f"{name} = kun::{op}({name}, kun::df_prod({fac[0]}, {fac[1]}));"
+                    fn = "df_acc_prod_neg" if which == "old" else "df_acc_prod"
+                    upd = f"kun::{fn}({name}, {fac[0]}, {fac[1]});"
                 L.append(f"{ind}if ({ok}) {upd}")
 
-    def _slide_value(self, i: int) -> str:
+    def _slide_value(self, i: int, ind: str) -> str:
         """The expanded window polynomial, evaluated in two-float arithmetic
-        from the window sums and the invariants, rounded once; NaN while a
-        row of the window has a NaN operand."""
+        from the window sums and the invariants (each term a window sum
+        scaled by the invariants and the coefficient, accumulated with
+        TwoSum), rounded once; NaN while a row of the window has a NaN
+        operand."""
         op, T = self.ops[i], self.T
         ns, w = op["nsrc"], op["window"]
         srcs, invs = op["in"][:ns], op["in"][ns:]
-        acc = None
+        acc = f"pa{i}"
+        self.lines.append(f"{ind}kun::DFloat {acc};")
         for c, se, ie in op["terms"]:
             mono = self._mono(srcs, se)
-            f = [self.mom[("s", mono, w)] if mono else f"kun::DFloat({float(w)!r}f)"]
+            term = self.mom[("s", mono, w)] if mono else f"kun::DFloat({float(w)!r}f)"
             for x, e in zip(invs, ie):
-                f += [f"kun::DFloat({self.val(x)})"] * e
+                for _ in range(e):
+                    term = f"kun::df_scale({term}, {self.val(x)})"
             if c != 1:
-                f.append(f"kun::DFloat({float(c)!r}f)")
-            term = f[0]
-            for g in f[1:]:
-                term = f"kun::kmul({term}, {g})"
-            acc = term if acc is None else f"kun::kadd({acc}, {term})"
+                term = f"kun::df_scale({term}, {float(c)!r}f)"
+            self.lines.append(f"{ind}kun::df_acc_pair({acc}, {term});")
         ok = " && ".join(f"{self.mom[('nn', x, w)]} == 0" for x in sorted(set(srcs)))
-        return f"(({ok}) ? ({T})({acc}) : kun::knan<{T}>())"
+        return f"(({ok}) ? ({T}){acc} : kun::knan<{T}>())"
 
     def _reg_window(self, i: int) -> bool:
         return self.ops[i]["window"] <= REG_WINDOW_MAX
@@ -977,7 +982,7 @@ class LeveledGen(StageGen):
         if self.slide:
             # chunked scans have threads enough to hide memory latency; keep
             # the registers for the window sums (single-buffered)
-            return 4
+            return SLIDE_BLOCK
         return SCAN_BLOCK if n <= 6 else (8 if n <= 12 else 4)
 
     def _scan_prefetch(self, role: dict, B: int, ind: str, chunk: bool = False):
@@ -1059,13 +1064,22 @@ class LeveledGen(StageGen):
         self.chunk_mode = chunk
         if self.slide:
             self._moment_updates(bj)
+        if chunk:
+            # warm-up rows only advance the states
+            L.append(f"{bj}if (t < t0) {{")
+            for i in sorted(comp):
+                if ops[i]["k"] in ("WindowedLinearRegression", "FastWindowedSum") and ops[i].get("p", -1) < 0 \
+                        and not (self.slide and ops[i]["k"] == "FastWindowedSum"):
+                    self.emit_top(i, bj + "  ", {}, comp)
+            L.append(f"{bj}  continue;")
+            L.append(f"{bj}}}")
         loops = self._loops()
         for i in range(len(ops)):
             if i in comp and ops[i].get("p", -1) < 0:
                 self.emit_top(i, bj, loops, comp)
         self.pf_window = None
         self.chunk_mode = False
-        guard = "if (t >= t0) " if chunk else ""
+        guard = ""
         for i in stores:
             L.append(f"{bj}{guard}b{i}[t * st{i}] = {self.val(i)};")
         L.append(f"{bi}}}")
