@@ -527,13 +527,15 @@ template <int W> struct SlideLinReg {
         return __fdiv_rn(__fmul_rn(r, r), __fmul_rn(varx(), (float)vy));
     }
     __device__ __forceinline__ float slope() const { return __fdiv_rn((float)cov(), varx()); }
-    // val - (slope*W + ym - slope*xm) = (N*val - ysum - slope*(W*N - xsum)) / N
+    // val - (slope*W + ym - slope*xm) = (N*val - ysum - slope*(W*N - xsum)) / N,
+    // with the slope kept as a pair: the residual is a small difference of
+    // large terms
     __device__ __forceinline__ float resi(float val) const {
         const float N = n();
-        const float s = slope();
+        const DFloat sd = kdiv(cov(), DFloat(varx()));
         DFloat r = df_prod(N, val);
         df_acc_pair(r, -ysum);
-        df_acc_pair(r, -df_prod(s, __fsub_rn(__fmul_rn((float)W, N), xsum)));
+        df_acc_pair(r, -kmul(sd, DFloat(__fsub_rn(__fmul_rn((float)W, N), xsum))));
         return __fdiv_rn((float)r, N);
     }
 };
