@@ -518,12 +518,17 @@ class LeveledGen(StageGen):
     def _kernels(self):
         plan, ops, lv = self.plan, self.ops, self.plan.lv
         ks = []
+        prev_cscans: List[dict] = []
         for L in plan.levels:
             if L % 2 == 0:
                 roots = [i for i in range(len(ops)) if plan.is_anchor(i) and lv[i] == L
                          and ops[i]["k"] not in SEQ]
-                for role in self._par_roles(roots, L):
-                    ks.append(dict(role, level=L, kind="par"))
+                if self.slide and prev_cscans:
+                    roots = self._fuse_into_scans(roots, L, prev_cscans)
+                prev_cscans = []
+                if roots:
+                    for role in self._par_roles(roots, L):
+                        ks.append(dict(role, level=L, kind="par"))
             else:
                 roles = []
                 for i in range(len(ops)):
@@ -537,17 +542,48 @@ class LeveledGen(StageGen):
                     roots = sorted(j for j in mem if ops[j]["k"] in ACC)
                     comp, vr, wr = plan.closure(roots, L)
                     roles.append({"roots": roots, "comp": comp, "vr": vr, "wr": wr})
+                prev_cscans = []
                 if roles and self.slide:
                     whole = []
                     for r in self._slide_roles(roles, L):
                         if self._chunkable(r):
                             ks.append({"level": L, "kind": "cscan", "roles": [r]})
+                            prev_cscans.append(r)
                         else:
                             whole.append(r)
                     roles = whole
                 if roles:
                     ks.append({"level": L, "kind": "scan", "roles": roles})
         return ks
+
+    def _fuse_into_scans(self, roots: List[int], L: int, scans: List[dict]) -> List[int]:
+        """Slide form: an output of level L that is a pointwise function of
+        one chunked scan's values (of level L - 1) and of series already in
+        memory is computed and stored by that scan, so the scan's values are
+        not written to memory and read back.  Returns the roots left."""
+        plan, ops, lv = self.plan, self.ops, self.plan.lv
+        left = []
+        for r in roots:
+            target = None
+            if ops[r]["k"] == "Output" and r not in self.plan._windowed_outputs:
+                try:
+                    comp, vr, wr = plan.closure([r], L)
+                except Unsupported:
+                    comp, vr, wr = set(), set(), {None}
+                pointwise = not wr and all(j == r or not plan.is_anchor(j) for j in comp)
+                need = {j for j in vr if lv[j] == L - 1}
+                if pointwise and need:
+                    for sc in scans:
+                        if need <= sc["comp"]:
+                            target = sc
+                            break
+            if target is None:
+                left.append(r)
+                continue
+            lv[r] = L - 1
+            target["roots"] = sorted(set(target["roots"]) | {r})
+            target["comp"], target["vr"], target["wr"] = plan.closure(target["roots"], L - 1)
+        return left
 
     def _chunkable(self, role: dict) -> bool:
         """A scan role whose states all forget rows older than their window
@@ -1299,7 +1335,8 @@ class LeveledGen(StageGen):
                 # its longest window; the tile is a launch parameter like a
                 # time-parallel kernel's
                 r = kd["roles"][0]
-                rr = r["vr"] | r["wr"] | {i for i in r["roots"] if i in self.scratch}
+                rr = (r["vr"] | r["wr"] | {i for i in r["roots"] if i in self.scratch}
+                      | {i for i in r["comp"] if ops[i]["k"] in ("Output", "WindowedTempOutput")})
                 for j in sorted(rr):
                     self._mem_ptr(j, decl, seen)
                 wmax = max(ops[i]["window"] for i in r["comp"] if ops[i]["k"] in FINITE_SEQ)
