@@ -75,4 +75,4 @@ def test_slide_specs_plan_and_generate(key, tmp_path):
     paths = codegen.generate_module(spec, str(tmp_path), tag=spec["name"])
     src = "".join(open(p).read() for p in paths)
     # the window moments are two-float sliding sums in time-chunked scans
-    assert "kun::df_prod(" in src and "const long long tw = t0 >" in src
+    assert "kun::df_acc_prod(" in src and "const long long tw = t0 >" in src
