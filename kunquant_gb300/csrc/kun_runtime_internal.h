@@ -156,11 +156,29 @@ struct TickSchedule {
 bool make_tick_schedule(const KunGpuModuleDesc *m, const std::vector<int> &order, int nstreams, TickSchedule &s);
 void free_tick_schedule(TickSchedule &s);
 
+// A tick as a chain of stage-graph levels: level d holds the stages whose
+// longest path from a source has d stages, so the stages of a level do not
+// depend on each other.  The Rank stages of a level run as one launch over
+// (segment, stage) blocks; every other stage keeps its own launch.  All on
+// one stream: a tick is a short chain of launches instead of one launch per
+// stage with cross-stream events.
+struct TickLevels {
+    std::vector<std::vector<int>> other;  // per level: non-Rank stages
+    std::vector<int> rank_off, rank_cnt;  // per level: slice of the job table
+    void *d_jobs = nullptr;               // device RankJob table
+    bool ok = false;
+};
+// false when a Rank stage does not read and write exactly one ring
+bool make_tick_levels(const StreamStore &store, const std::vector<int> &order, TickLevels &lv);
+void free_tick_levels(TickLevels &lv);
+
 // Enqueue one tick of every stage of `store` for the segments described by
 // the device arrays; with `d_seg_count` the host counts are upper bounds.
+// With `levels` the tick runs level by level on `st` (TickLevels), else
+// stage by stage on `sched`'s streams (or on `st` alone).
 KunStatus enqueue_tick(const StreamStore &store, const std::vector<int> &order, const int32_t *d_seg_off,
                        const int32_t *d_seg_stock0, const int64_t *d_tick, int nseg, long long n_active,
                        int max_len, cudaStream_t st, const int32_t *d_seg_count = nullptr,
-                       const TickSchedule *sched = nullptr);
+                       const TickSchedule *sched = nullptr, const TickLevels *levels = nullptr);
 
 }  // namespace kungpu

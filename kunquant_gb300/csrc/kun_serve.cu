@@ -105,6 +105,7 @@ struct ServePool {
     uint64_t steps = 0;
     std::map<std::pair<long long, int>, cudaGraphExec_t> graphs;
     TickSchedule sched;            // concurrent stages inside the step graph
+    TickLevels levels;             // the step as a chain of stage-graph levels
     std::mutex mu;                 // sessions, columns, queue
     std::mutex gpu_mu;             // one step on the device at a time
     // request loop (continuous batching)
@@ -142,6 +143,7 @@ ServePool::~ServePool() {
     cudaStreamSynchronize(stream());
     for (auto &g : graphs) cudaGraphExecDestroy(g.second);
     free_tick_schedule(sched);
+    free_tick_levels(levels);
     void *dev[] = {d_table, d_in_rings, d_out_rings, d_in_win, d_out_win, d_in, d_out};
     for (void *q : dev)
         if (q) cudaFree(q);
@@ -178,7 +180,7 @@ static KunStatus build_serve_graph(ServePool *p, long long nb, int sb, cudaGraph
         serve_scatter<double><<<gin, 256, 0, st>>>((const double *)p->d_in, (double *const *)p->d_in_rings,
                                                    p->d_in_win, p->off(), p->stock0(), p->ticks(), p->cnt(), p->cap);
     KunStatus rs = enqueue_tick(p->store, p->order, p->off(), p->stock0(), (const int64_t *)p->ticks(), sb, nb,
-                                p->max_len, st, p->cnt(), &p->sched);
+                                p->max_len, st, p->cnt(), &p->sched, &p->levels);
     if (!p->out_bufs.empty()) {
         if (p->elem() == 4)
             serve_gather<float><<<gout, 256, 0, st>>>((float *)p->d_out, (float *const *)p->d_out_rings,
@@ -473,6 +475,12 @@ KUN_EXPORT KunStatus kunCreateServePool(KunExecutorHandle exec, KunModuleHandle 
         return KUN_OUT_OF_MEMORY;
     }
     memset(p->h_table, 0, p->table_bytes);
+    // a module whose Rank stages do not fit the level form keeps the
+    // stage-by-stage schedule
+    if (!make_tick_levels(p->store, p->order, p->levels)) {
+        cudaGetLastError();
+        free_tick_levels(p->levels);
+    }
     std::vector<void *> rin, rout;
     std::vector<int32_t> win, wout;
     for (int b : p->in_bufs) {

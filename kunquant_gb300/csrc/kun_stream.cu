@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "kun_runtime_internal.h"
+#include "kun_xsec.cuh"
 
 namespace kungpu {
 
@@ -179,10 +180,120 @@ void free_tick_schedule(TickSchedule &s) {
 // Enqueue one tick of every stage for the segments in d_seg / d_tick: in
 // order on `st`, or with `sched`, on its streams (forked from and joined back
 // into `st`) with events for the cross-stream dependencies.
+bool make_tick_levels(const StreamStore &store, const std::vector<int> &order, TickLevels &lv) {
+    const KunGpuModuleDesc *m = store.m;
+    const int ns = m->num_stages;
+    std::vector<int> depth(ns, 0);
+    for (int si : order)  // a topological order: predecessors come first
+        for (int d = 0; d < m->stages[si].num_deps; d++) {
+            const int j = m->stages[si].deps[d];
+            if (j >= 0) depth[j] = std::max(depth[j], depth[si] + 1);
+        }
+    int nl = 0;
+    for (int si : order) nl = std::max(nl, depth[si] + 1);
+    std::vector<std::vector<int>> ranks(nl);
+    lv.other.assign(nl, {});
+    for (int si : order) {
+        const KunGpuStageDesc &d = m->stages[si];
+        if (d.kind == KUN_STAGE_RANK) {
+            if (d.num_in != 1 || d.num_out != 1) return false;
+            ranks[depth[si]].push_back(si);
+        } else {
+            lv.other[depth[si]].push_back(si);
+        }
+    }
+    std::vector<kun::RankJob> jobs;
+    lv.rank_off.assign(nl, 0);
+    lv.rank_cnt.assign(nl, 0);
+    for (int l = 0; l < nl; l++) {
+        lv.rank_off[l] = (int)jobs.size();
+        lv.rank_cnt[l] = (int)ranks[l].size();
+        for (int si : ranks[l]) {
+            const int bi = m->stages[si].in_bufs[0], bo = m->stages[si].out_bufs[0];
+            kun::RankJob jb;
+            jb.in = store.rings[bi];
+            jb.out = store.rings[bo];
+            jb.w_in = std::max(1, (int)m->buffers[bi].window);
+            jb.w_out = std::max(1, (int)m->buffers[bo].window);
+            jobs.push_back(jb);
+        }
+    }
+    if (!jobs.empty()) {
+        if (cudaMalloc(&lv.d_jobs, jobs.size() * sizeof(kun::RankJob)) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (cudaMemcpy(lv.d_jobs, jobs.data(), jobs.size() * sizeof(kun::RankJob), cudaMemcpyHostToDevice) !=
+            cudaSuccess)
+            return false;
+    }
+    lv.ok = true;
+    return true;
+}
+
+void free_tick_levels(TickLevels &lv) {
+    if (lv.d_jobs) cudaFree(lv.d_jobs);
+    lv.d_jobs = nullptr;
+    lv.ok = false;
+}
+
+static KunStatus launch_stage(const StreamStore &store, int si, const int32_t *d_seg_off, const int32_t *d_seg_stock0,
+                              const int64_t *d_tick, int nseg, long long n_active, int max_len, cudaStream_t sst,
+                              const int32_t *d_seg_count) {
+    const KunGpuStageDesc &d = store.m->stages[si];
+    KunGpuStageArgs a;
+    memset(&a, 0, sizeof a);
+    a.buffers = store.rings.data();
+    a.num_stocks = store.cap;
+    a.total_time = 1;
+    a.length = 1;
+    a.state = store.st_t[si];
+    a.state_i = store.st_i[si];
+    a.seg_off = d_seg_off;
+    a.seg_stock0 = d_seg_stock0;
+    a.seg_tick = d_tick;
+    a.nseg = nseg;
+    a.n_active = n_active;
+    a.max_seg_len = max_len;
+    a.seg_count = d_seg_count;
+    int rc = d.launch(&a, (void *)sst);
+    if (rc) {
+        set_error("stage %d (%s) failed: %s", si, d.name, cudaGetErrorString((cudaError_t)rc));
+        return KUN_CUDA_ERROR;
+    }
+    return KUN_SUCCESS;
+}
+
 KunStatus enqueue_tick(const StreamStore &store, const std::vector<int> &order, const int32_t *d_seg_off,
                        const int32_t *d_seg_stock0, const int64_t *d_tick, int nseg, long long n_active,
-                       int max_len, cudaStream_t st, const int32_t *d_seg_count, const TickSchedule *sched) {
+                       int max_len, cudaStream_t st, const int32_t *d_seg_count, const TickSchedule *sched,
+                       const TickLevels *levels) {
     const KunGpuModuleDesc *m = store.m;
+    if (levels && levels->ok) {
+        for (size_t l = 0; l < levels->other.size(); l++) {
+            for (int si : levels->other[l]) {
+                KunStatus rs = launch_stage(store, si, d_seg_off, d_seg_stock0, d_tick, nseg, n_active, max_len, st,
+                                            d_seg_count);
+                if (rs != KUN_SUCCESS) return rs;
+            }
+            if (levels->rank_cnt[l] > 0) {
+                const kun::RankJob *jobs = (const kun::RankJob *)levels->d_jobs + levels->rank_off[l];
+                int rc = m->dtype == 0
+                             ? kun::launch_rank_multi_segments<float>(jobs, levels->rank_cnt[l], store.cap, d_seg_off,
+                                                                      d_seg_stock0, (const long long *)d_tick, nseg,
+                                                                      max_len, d_seg_count, st)
+                             : kun::launch_rank_multi_segments<double>(jobs, levels->rank_cnt[l], store.cap,
+                                                                       d_seg_off, d_seg_stock0,
+                                                                       (const long long *)d_tick, nseg, max_len,
+                                                                       d_seg_count, st);
+                if (rc) {
+                    set_error("rank stages of level %d failed: %s", (int)l, cudaGetErrorString((cudaError_t)rc));
+                    return KUN_CUDA_ERROR;
+                }
+            }
+        }
+        return KUN_SUCCESS;
+    }
     const bool multi = sched && sched->streams.size() > 1;
     if (multi) {
         cudaEventRecord(sched->fork, st);
@@ -257,9 +368,11 @@ struct StreamCtx {
     std::vector<int> last_row;
     std::vector<std::vector<char>> mirror;
     cudaGraphExec_t graph = nullptr;
+    TickLevels levels;
     cudaStream_t stream() const { return ex->streams[0]; }
     ~StreamCtx() {
         if (graph) cudaGraphExecDestroy(graph);
+        free_tick_levels(levels);
         if (d_seg) cudaFree(d_seg);
         if (d_tick) cudaFree(d_tick);
         store.release();
@@ -274,7 +387,8 @@ static KunStatus build_graph(StreamCtx *c) {
         set_error("cannot capture the tick graph");
         return KUN_CUDA_ERROR;
     }
-    KunStatus rs = enqueue_tick(c->store, c->order, c->d_seg, c->d_seg + 2, c->d_tick, 1, c->S, (int)c->S, st);
+    KunStatus rs = enqueue_tick(c->store, c->order, c->d_seg, c->d_seg + 2, c->d_tick, 1, c->S, (int)c->S, st,
+                                nullptr, nullptr, &c->levels);
     advance_tick<<<1, 32, 0, st>>>((long long *)c->d_tick, 1);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
@@ -550,6 +664,10 @@ static StreamCtx *create_ctx(Executor *ex, const KunGpuModuleDesc *m, long long 
         set_error("out of device memory for a stream of %lld stocks", S);
         delete c;
         return nullptr;
+    }
+    if (!make_tick_levels(c->store, c->order, c->levels)) {
+        cudaGetLastError();
+        free_tick_levels(c->levels);
     }
     cudaStream_t st = c->stream();
     int32_t seg[3] = {0, (int32_t)S, 0};

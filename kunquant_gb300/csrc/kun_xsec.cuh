@@ -482,6 +482,42 @@ __global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restric
         rank_one_row<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, Pk, keys, cnt_warp);
 }
 
+// Stream mode, several Rank stages at once: block (k, j) ranks segment k
+// for stage j of the job table (the stages of one level of the stage graph,
+// which do not depend on each other).  Each job names the stage's input and
+// output rings; the segment table is the step's.
+struct RankJob {
+    const void *in;
+    void *out;
+    int32_t w_in, w_out;
+};
+
+template <typename T, int ITEMS>
+__global__ void __launch_bounds__(kRankThreads) rank_multi_segments(const RankJob *__restrict__ jobs, long long cap,
+                                                                    const int32_t *seg_off, const int32_t *seg_stock0,
+                                                                    const long long *seg_tick, int P,
+                                                                    const int32_t *cnt) {
+    using K = typename SortKey<T>::K;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int cnt_warp[kRankThreads / 32];
+    const int k = blockIdx.x;
+    if (cnt && k >= cnt[0]) return;
+    const RankJob jb = jobs[blockIdx.y];
+    const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
+    if (len > P || len <= 0) return;
+    int Pk = ITEMS;
+    while (Pk < len) Pk <<= 1;
+    const T *in = (const T *)jb.in + (n % jb.w_in) * cap + s0;
+    T *out = (T *)jb.out + (n % jb.w_out) * cap + s0;
+    K *keys = reinterpret_cast<K *>(smem_raw);
+    uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
+    if (Pk >= kRadixMinP)
+        rank_one_row_radix<T, ITEMS>(in, out, len, keys, counters, idx, cnt_warp);
+    else
+        rank_one_row<T, ITEMS>(in, out, len, Pk, keys, cnt_warp);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(256) scale_rows(const T *__restrict__ in, T *__restrict__ out, long long S,
                                                   long long length) {
@@ -691,6 +727,32 @@ inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long l
     case 8: return go(rank_segments<T, 8>);
     case 16: return go(rank_segments<T, 16>);
     default: return go(rank_segments<T, 32>);
+    }
+}
+
+// njobs Rank stages over the step's segments in one launch
+template <typename T>
+inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long long cap, const int32_t *seg_off,
+                                      const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
+                                      const int32_t *cnt, cudaStream_t st) {
+    if (njobs <= 0 || nseg <= 0) return 0;
+    int P = 8;
+    while (P < max_len) P <<= 1;
+    size_t smem = rank_smem_bytes<T>(P);
+    if (smem > 227 * 1024 || P > 32 * kRankThreads || njobs > 65535) return (int)cudaErrorInvalidValue;
+    auto go = [&](auto kernel) {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return (int)e;
+        }
+        kernel<<<dim3((unsigned)nseg, (unsigned)njobs), kRankThreads, smem, st>>>(d_jobs, cap, seg_off, seg_stock0,
+                                                                                 seg_tick, P, cnt);
+        return (int)cudaGetLastError();
+    };
+    switch (rank_items(P)) {
+    case 8: return go(rank_multi_segments<T, 8>);
+    case 16: return go(rank_multi_segments<T, 16>);
+    default: return go(rank_multi_segments<T, 32>);
     }
 }
 
