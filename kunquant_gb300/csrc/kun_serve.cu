@@ -27,6 +27,7 @@
 #include <vector>
 
 #include "kun_runtime_internal.h"
+#include "kun_xsec.cuh"
 
 namespace kungpu {
 
@@ -238,7 +239,7 @@ static KunStatus run_step(ServePool *p, const StepShape &sh, const void *dev_in,
     cudaStream_t st = p->stream();
     size_t elem = p->elem();
     // the table goes as two copies: ints up to cnt, then the ticks
-    cudaMemcpyAsync(p->d_table, p->h_table, (2 * p->max_sessions + 4) * sizeof(int32_t), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(p->d_table, p->h_table, (2 * p->max_sessions + 5) * sizeof(int32_t), cudaMemcpyHostToDevice, st);
     cudaMemcpyAsync(p->d_table + p->tick_off, p->h_table + p->tick_off, sh.nsess * sizeof(long long),
                     cudaMemcpyHostToDevice, st);
     // every input and output row moves as 2D copies: one over the column
@@ -312,6 +313,14 @@ static KunStatus prepare_step(ServePool *p, int nsess, const int64_t *sids, std:
         }
         s.stamp = stamp;
         sel[k] = &s;
+    }
+    // the sessions the small Rank blocks serve come first (cnt[3] of them)
+    std::stable_partition(sel.begin(), sel.end(),
+                          [](const Session *q) { return q->len <= (long long)kun::kRankSmallMax; });
+    int nsmall = 0;
+    for (int k = 0; k < nsess; k++) {
+        Session &s = *sel[k];
+        nsmall += s.len <= (long long)kun::kRankSmallMax;
         off[k] = (int32_t)n;
         s0[k] = (int32_t)s.stock0;
         tk[k] = s.tick;
@@ -337,6 +346,7 @@ static KunStatus prepare_step(ServePool *p, int nsess, const int64_t *sids, std:
     cnt[0] = nsess;
     cnt[1] = (int32_t)n;
     cnt[2] = longest;
+    cnt[3] = nsmall;
     sh.nsess = nsess;
     sh.n = n;
     sh.lo = lo;
@@ -455,7 +465,7 @@ KUN_EXPORT KunStatus kunCreateServePool(KunExecutorHandle exec, KunModuleHandle 
         if (m->buffers[b].kind == KUN_BUF_OUTPUT) p->out_bufs.push_back(b);
     }
     size_t elem = p->elem();
-    size_t ints = (size_t)(2 * max_sessions + 4);
+    size_t ints = (size_t)(2 * max_sessions + 5);
     p->tick_off = (ints * sizeof(int32_t) + 15) / 16 * 16;
     p->table_bytes = p->tick_off + (size_t)max_sessions * sizeof(long long);
     size_t nin = p->in_bufs.size(), nout = p->out_bufs.size();

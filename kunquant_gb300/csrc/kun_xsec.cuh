@@ -492,19 +492,25 @@ struct RankJob {
     int32_t w_in, w_out;
 };
 
-template <typename T, int ITEMS>
-__global__ void __launch_bounds__(kRankThreads) rank_multi_segments(const RankJob *__restrict__ jobs, long long cap,
-                                                                    const int32_t *seg_off, const int32_t *seg_stock0,
-                                                                    const long long *seg_tick, int P,
-                                                                    const int32_t *cnt) {
+// Segments of at most kRankSmallMax stocks go to blocks of kRankSmallThreads
+// threads (a bitonic sort of at most 1024 keys, 8 per thread); longer ones to
+// kRankThreads-thread blocks.  A step's table lists its small segments first
+// and holds their number in cnt[3].
+constexpr int kRankSmallMax = 1024;
+constexpr int kRankSmallThreads = kRankSmallMax / 8;
+
+template <typename T, int ITEMS, bool SMALL>
+__global__ void __launch_bounds__(SMALL ? kRankSmallThreads : kRankThreads)
+    rank_multi_segments(const RankJob *__restrict__ jobs, long long cap, const int32_t *seg_off,
+                        const int32_t *seg_stock0, const long long *seg_tick, int P, const int32_t *cnt) {
     using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
     const int k = blockIdx.x;
-    if (cnt && k >= cnt[0]) return;
+    if (cnt && (k >= cnt[0] || (SMALL ? k >= cnt[3] : k < cnt[3]))) return;
     const RankJob jb = jobs[blockIdx.y];
     const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
-    if (len > P || len <= 0) return;
+    if (len > P || len <= 0 || (SMALL && len > kRankSmallMax)) return;
     int Pk = ITEMS;
     while (Pk < len) Pk <<= 1;
     const T *in = (const T *)jb.in + (n % jb.w_in) * cap + s0;
@@ -512,7 +518,9 @@ __global__ void __launch_bounds__(kRankThreads) rank_multi_segments(const RankJo
     K *keys = reinterpret_cast<K *>(smem_raw);
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
-    if (Pk >= kRadixMinP)
+    if (SMALL)
+        rank_one_row<T, ITEMS>(in, out, len, Pk, keys, cnt_warp);
+    else if (Pk >= kRadixMinP)
         rank_one_row_radix<T, ITEMS>(in, out, len, keys, counters, idx, cnt_warp);
     else
         rank_one_row<T, ITEMS>(in, out, len, Pk, keys, cnt_warp);
@@ -730,29 +738,41 @@ inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long l
     }
 }
 
-// njobs Rank stages over the step's segments in one launch
+// njobs Rank stages over the step's segments: one launch for the segments
+// of at most kRankSmallMax stocks and one for the longer ones.  With a
+// device table (cnt: nseg, stocks, longest, number of small segments) both
+// launch and each takes its part; without one every segment goes to the
+// launch that max_len picks.
 template <typename T>
 inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long long cap, const int32_t *seg_off,
                                       const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
                                       const int32_t *cnt, cudaStream_t st) {
     if (njobs <= 0 || nseg <= 0) return 0;
+    if (njobs > 65535) return (int)cudaErrorInvalidValue;
+    const dim3 grid((unsigned)nseg, (unsigned)njobs);
+    if (cnt || max_len <= kRankSmallMax) {
+        const size_t smem = rank_smem_bytes<T>(kRankSmallMax);
+        rank_multi_segments<T, 8, true><<<grid, kRankSmallThreads, smem, st>>>(d_jobs, cap, seg_off, seg_stock0,
+                                                                            seg_tick, kRankSmallMax, cnt);
+        if (cudaError_t e = cudaGetLastError()) return (int)e;
+    }
+    if (!cnt && max_len <= kRankSmallMax) return 0;
     int P = 8;
     while (P < max_len) P <<= 1;
     size_t smem = rank_smem_bytes<T>(P);
-    if (smem > 227 * 1024 || P > 32 * kRankThreads || njobs > 65535) return (int)cudaErrorInvalidValue;
+    if (smem > 227 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
     auto go = [&](auto kernel) {
         if (smem > 48 * 1024) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return (int)e;
         }
-        kernel<<<dim3((unsigned)nseg, (unsigned)njobs), kRankThreads, smem, st>>>(d_jobs, cap, seg_off, seg_stock0,
-                                                                                 seg_tick, P, cnt);
+        kernel<<<grid, kRankThreads, smem, st>>>(d_jobs, cap, seg_off, seg_stock0, seg_tick, P, cnt);
         return (int)cudaGetLastError();
     };
     switch (rank_items(P)) {
-    case 8: return go(rank_multi_segments<T, 8>);
-    case 16: return go(rank_multi_segments<T, 16>);
-    default: return go(rank_multi_segments<T, 32>);
+    case 8: return go(rank_multi_segments<T, 8, false>);
+    case 16: return go(rank_multi_segments<T, 16, false>);
+    default: return go(rank_multi_segments<T, 32, false>);
     }
 }
 

@@ -90,6 +90,34 @@ def test_pool_mix_equals_alone(name):
 
 
 @pytest.mark.gpu
+def test_pool_rank_size_classes():
+    """Sessions on both sides of the small-segment Rank threshold (1024
+    stocks: 128-thread blocks below, 1024-thread blocks with the radix sort
+    above) in one step, each equal to its StreamContext run alone."""
+    mod = _module("alpha101_stream")
+    ex = kr.createSingleThreadExecutor()
+    T = 40
+    sizes = [1024, 1025, 40, 3000, 700]
+    data = [_data(mod, S, T, seed=300 + i) for i, S in enumerate(sizes)]
+    want = [_alone(ex, mod, d) for d in data]
+    pool = serve.ServePool(ex, mod, capacity_stocks=sum(sizes), max_sessions=8, max_session_stocks=3000,
+                           start=False)
+    sess = [pool.try_open(S) for S in sizes]
+    got = [{k: np.empty((T, S), mod.dtype) for k in mod.getOutputNames()} for S in sizes]
+    for t in range(T):
+        for i, se in enumerate(sess):
+            for k in mod.getInputNames():
+                se.inputs[k][:] = data[i][k][t]
+        pool.step(sess[::-1])
+        for i, se in enumerate(sess):
+            for k in mod.getOutputNames():
+                got[i][k][t] = se.outputs[k]
+    for i in range(len(sizes)):
+        assert not compare_exact(got[i], want[i]), f"session of {sizes[i]} stocks differs from its StreamContext run"
+    pool.shutdown()
+
+
+@pytest.mark.gpu
 def test_pool_request_loop_threads():
     """Ticks submitted from several client threads through the request loop
     give the same outputs as the sessions run alone."""
