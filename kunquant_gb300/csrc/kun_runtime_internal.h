@@ -166,6 +166,10 @@ struct TickLevels {
     std::vector<std::vector<int>> other;  // per level: non-Rank stages
     std::vector<int> rank_off, rank_cnt;  // per level: slice of the job table
     void *d_jobs = nullptr;               // device RankJob table
+    // the Rank launch of long segments runs beside the short ones' on
+    // `side` (forked from and joined to the tick's stream at each level)
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     bool ok = false;
 };
 // false when a Rank stage does not read and write exactly one ring

@@ -227,13 +227,22 @@ bool make_tick_levels(const StreamStore &store, const std::vector<int> &order, T
             cudaSuccess)
             return false;
     }
+    if (cudaStreamCreateWithFlags(&lv.side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&lv.fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&lv.join, cudaEventDisableTiming) != cudaSuccess)
+        return false;
     lv.ok = true;
     return true;
 }
 
 void free_tick_levels(TickLevels &lv) {
     if (lv.d_jobs) cudaFree(lv.d_jobs);
+    if (lv.side) cudaStreamDestroy(lv.side);
+    if (lv.fork) cudaEventDestroy(lv.fork);
+    if (lv.join) cudaEventDestroy(lv.join);
     lv.d_jobs = nullptr;
+    lv.side = nullptr;
+    lv.fork = lv.join = nullptr;
     lv.ok = false;
 }
 
@@ -278,14 +287,26 @@ KunStatus enqueue_tick(const StreamStore &store, const std::vector<int> &order, 
             }
             if (levels->rank_cnt[l] > 0) {
                 const kun::RankJob *jobs = (const kun::RankJob *)levels->d_jobs + levels->rank_off[l];
+                // with a device table both size classes launch: the long
+                // segments' launch on the side stream, concurrently
+                const bool both = d_seg_count != nullptr && max_len > kun::kRankSmallMax;
+                if (both) {
+                    cudaEventRecord(levels->fork, st);
+                    cudaStreamWaitEvent(levels->side, levels->fork, 0);
+                }
+                cudaStream_t sl = both ? levels->side : nullptr;
                 int rc = m->dtype == 0
                              ? kun::launch_rank_multi_segments<float>(jobs, levels->rank_cnt[l], store.cap, d_seg_off,
                                                                       d_seg_stock0, (const long long *)d_tick, nseg,
-                                                                      max_len, d_seg_count, st)
+                                                                      max_len, d_seg_count, st, sl)
                              : kun::launch_rank_multi_segments<double>(jobs, levels->rank_cnt[l], store.cap,
                                                                        d_seg_off, d_seg_stock0,
                                                                        (const long long *)d_tick, nseg, max_len,
-                                                                       d_seg_count, st);
+                                                                       d_seg_count, st, sl);
+                if (both) {
+                    cudaEventRecord(levels->join, levels->side);
+                    cudaStreamWaitEvent(st, levels->join, 0);
+                }
                 if (rc) {
                     set_error("rank stages of level %d failed: %s", (int)l, cudaGetErrorString((cudaError_t)rc));
                     return KUN_CUDA_ERROR;

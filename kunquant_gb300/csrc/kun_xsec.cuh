@@ -746,7 +746,7 @@ inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long l
 template <typename T>
 inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long long cap, const int32_t *seg_off,
                                       const int32_t *seg_stock0, const long long *seg_tick, int nseg, int max_len,
-                                      const int32_t *cnt, cudaStream_t st) {
+                                      const int32_t *cnt, cudaStream_t st, cudaStream_t st_long = nullptr) {
     if (njobs <= 0 || nseg <= 0) return 0;
     if (njobs > 65535) return (int)cudaErrorInvalidValue;
     const dim3 grid((unsigned)nseg, (unsigned)njobs);
@@ -757,6 +757,7 @@ inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long lon
         if (cudaError_t e = cudaGetLastError()) return (int)e;
     }
     if (!cnt && max_len <= kRankSmallMax) return 0;
+    if (st_long) st = st_long;
     int P = 8;
     while (P < max_len) P <<= 1;
     size_t smem = rank_smem_bytes<T>(P);
