@@ -4,7 +4,8 @@
 // length) of one batch module.  Stage by stage in the module's order, a
 // time-series stage that supports grouped launches runs each of its kernels
 // ONCE over the tiles of all jobs (the job of a block is found from a tile
-// table passed by value); other stages run job by job.  The jobs' parameter
+// table passed by value); a Rank stage ranks every job's rows in one launch;
+// other stages run job by job.  The jobs' parameter
 // blocks go to the device with one copy per stage.  This replaces the
 // reference's one runGraph per universe (cpp/Kun/Runtime.cpp:311-352).
 //
@@ -19,6 +20,7 @@
 #include <vector>
 
 #include "kun_runtime_internal.h"
+#include "kun_xsec.cuh"
 
 namespace kungpu {
 
@@ -167,6 +169,50 @@ static KunStatus batch_stage(BatchRun &br, int si, cudaStream_t st, const int32_
             a.tune_block = tn->second[si].block.data();
         }
     }
+    // Rank stages in the TS layout: every job's rows in one launch
+    const bool ts_rank = d.kind == KUN_STAGE_RANK && n > 1 && d.num_in == 1 && d.num_out == 1 &&
+                         (m->buffers[d.in_bufs[0]].kind != KUN_BUF_INPUT || m->input_layout == KUN_LAYOUT_TS) &&
+                         (m->buffers[d.out_bufs[0]].kind != KUN_BUF_OUTPUT || m->output_layout == KUN_LAYOUT_TS);
+    if (ts_rank) {
+        const int bi = d.in_bufs[0], bo = d.out_bufs[0];
+        const size_t esz = m->dtype == 0 ? 4 : 8;
+        std::vector<kun::RankRowsJob> jobs;
+        long long rows = 0, max_S = 0;
+        for (int j = 0; j < n; j++) {
+            const BatchJob &jb = br.jobs[j];
+            if (jb.S <= 0 || jb.length <= 0) continue;
+            kun::RankRowsJob rj;
+            const long long row_off = m->buffers[bi].kind == KUN_BUF_INPUT ? jb.cur_time : 0;
+            rj.in = (const char *)jb.ptrs[bi] + (size_t)row_off * (size_t)jb.S * esz;
+            rj.out = jb.ptrs[bo];
+            rj.S = jb.S;
+            rj.length = jb.length;
+            rj.row0 = rows;
+            rows += jb.length;
+            max_S = std::max(max_S, jb.S);
+            jobs.push_back(rj);
+        }
+        const size_t bytes = jobs.size() * sizeof(kun::RankRowsJob);
+        const size_t off = (br.host_off + 255) / 256 * 256;
+        if (off + bytes > ex->group_host_bytes) {
+            set_error("grouped launch staging exhausted");
+            return KUN_OUT_OF_MEMORY;
+        }
+        memcpy((char *)ex->group_host + off, jobs.data(), bytes);
+        char *dev = (char *)ex->group_dev.ptr + off;
+        cudaMemcpyAsync(dev, (char *)ex->group_host + off, bytes, cudaMemcpyHostToDevice, st);
+        int rc = m->dtype == 0 ? kun::launch_rank_rows_multi<float>((const kun::RankRowsJob *)dev, (int)jobs.size(),
+                                                                    rows, max_S, st)
+                               : kun::launch_rank_rows_multi<double>((const kun::RankRowsJob *)dev,
+                                                                     (int)jobs.size(), rows, max_S, st);
+        if (rc) {
+            set_error("stage %d (%s) grouped Rank failed: %s", si, d.name, cudaGetErrorString((cudaError_t)rc));
+            return KUN_CUDA_ERROR;
+        }
+        br.host_off = off + bytes;
+        launches += 1;
+        return KUN_SUCCESS;
+    }
     if (d.launch_group && n > 1) {
         for (int j0 = 0; j0 < n; j0 += KUN_GROUP_MAX) {
             const int nj = std::min(KUN_GROUP_MAX, n - j0);
@@ -207,6 +253,10 @@ static size_t batch_staging_bytes(const BatchRun &br) {
     const int n = (int)br.jobs.size();
     for (int si = 0; si < br.m->num_stages; si++) {
         const KunGpuStageDesc &d = br.m->stages[si];
+        if (d.kind == KUN_STAGE_RANK && n > 1) {  // the grouped Rank's job table
+            need += ((size_t)n * sizeof(kun::RankRowsJob) + 255) / 256 * 256;
+            continue;
+        }
         if (!d.launch_group || n <= 1) continue;
         std::vector<KunGpuStageArgs> args(n);
         memset(args.data(), 0, sizeof(KunGpuStageArgs) * n);

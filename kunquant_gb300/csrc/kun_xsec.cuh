@@ -682,6 +682,71 @@ inline int launch_rank_items(const T *in, T *out, long long S, long long length,
     return (int)cudaGetLastError();
 }
 
+// Batch runs of several universes: the rows of one Rank stage of every job
+// in one launch.  Job j ranks rows [row0, row0 + length) of the launch's
+// row space, reading `in` and writing `out` ([length][S], TS).
+struct RankRowsJob {
+    const void *in;
+    void *out;
+    long long S, length, row0;
+};
+
+template <typename T, int ITEMS>
+__global__ void __launch_bounds__(kRankThreads) rank_rows_multi(const RankRowsJob *__restrict__ jobs, int njobs,
+                                                                long long total_rows, int P) {
+    using K = typename SortKey<T>::K;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ int cnt_warp[kRankThreads / 32];
+    K *keys = reinterpret_cast<K *>(smem_raw);
+    uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
+    uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
+    for (long long r = blockIdx.x; r < total_rows; r += gridDim.x) {
+        int lo = 0, hi = njobs - 1;  // the job whose rows hold r
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (jobs[mid].row0 <= r) lo = mid;
+            else hi = mid - 1;
+        }
+        const RankRowsJob jb = jobs[lo];
+        const long long t = r - jb.row0, S = jb.S;
+        if (t < 0 || t >= jb.length || S <= 0 || S > P) continue;
+        const T *in = (const T *)jb.in + t * S;
+        T *out = (T *)jb.out + t * S;
+        int Pk = ITEMS;
+        while (Pk < S) Pk <<= 1;
+        if (Pk >= kRadixMinP)
+            rank_one_row_radix<T, ITEMS>(in, out, S, keys, counters, idx, cnt_warp);
+        else
+            rank_one_row<T, ITEMS>(in, out, S, Pk, keys, cnt_warp);
+    }
+}
+
+// max_S: the longest row of the jobs (sizes the keys per thread and the
+// shared memory)
+template <typename T>
+inline int launch_rank_rows_multi(const RankRowsJob *d_jobs, int njobs, long long total_rows, long long max_S,
+                                  cudaStream_t st) {
+    if (njobs <= 0 || total_rows <= 0) return 0;
+    int P = 8;
+    while (P < max_S) P <<= 1;
+    const size_t smem = rank_smem_bytes<T>(P);
+    if (smem > 227 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
+    const long long grid = total_rows < (long long)kun_num_sms() * 2 ? total_rows : (long long)kun_num_sms() * 2;
+    auto go = [&](auto kernel) {
+        if (smem > 48 * 1024) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return (int)e;
+        }
+        kernel<<<(unsigned)grid, kRankThreads, smem, st>>>(d_jobs, njobs, total_rows, P);
+        return (int)cudaGetLastError();
+    };
+    switch (rank_items(P)) {
+    case 8: return go(rank_rows_multi<T, 8>);
+    case 16: return go(rank_rows_multi<T, 16>);
+    default: return go(rank_rows_multi<T, 32>);
+    }
+}
+
 template <typename T>
 inline int launch_rank(const T *in, T *out, long long S, long long length, cudaStream_t st) {
     int P = 8;
