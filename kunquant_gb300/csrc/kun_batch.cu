@@ -161,6 +161,7 @@ static KunStatus batch_stage(BatchRun &br, int si, cudaStream_t st, const int32_
         a.total_time = jb.total_time;
         a.start = jb.cur_time;
         a.length = jb.length;
+        a.error_flag = ex->d_error;
         if (tile) {
             a.tune_tile = tile;
             a.tune_block = block;

@@ -5,6 +5,7 @@
 // -fmad=false: a product is fused into an add only where a template below
 // calls kfma(), which is exactly where the reference's GCC build forms an FMA.
 #pragma once
+#include <cstdlib>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -45,6 +46,63 @@ __device__ __forceinline__ T ldw(const T* __restrict__ p, long long st, long lon
     if (EDGE) return (unsigned long long)row < (unsigned long long)length ? p[row * st] : knan<T>();
     return p[row * st];
 }
+// ---------------- bulk async copies (TMA) into shared memory, on mbarriers
+// One thread of a block issues cp.async.bulk copies of whole rows (16-byte
+// aligned, sizes multiples of 16) into a shared-memory stage and tells the
+// stage's mbarrier how many bytes to expect; every thread waits on the
+// barrier's phase before reading the stage.  Waits are bounded.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// makes the initialised barriers visible to the async proxy
+__device__ __forceinline__ void mbar_init_fence() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy (bulk copy) writes
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32_t bytes, unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// waits for the barrier's phase `parity` to complete; false after `limit`
+// polls (each try_wait itself suspends for a while)
+__device__ __forceinline__ bool mbar_wait(unsigned long long *bar, uint32_t parity, int limit) {
+    for (int i = 0; i < limit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+constexpr int kTmaWaitLimit = 1 << 20;
+// the staged (bulk-copy) instance of an elementwise kernel is used unless
+// KUN_NO_TMA is set in the environment (read once)
+inline bool tma_enabled() {
+    static const bool on = std::getenv("KUN_NO_TMA") == nullptr;
+    return on;
+}
+inline bool aligned16(const void *p) { return ((unsigned long long)p & 15ull) == 0; }
+constexpr int kTmaRows = 4;  // rows of every input series per stage
+
 // ring row of the value `off` ticks back, given this tick's row nm (0 <= off < W)
 __device__ __forceinline__ int ring_row(int nm, int off, int W) {
     const int r = nm - off;

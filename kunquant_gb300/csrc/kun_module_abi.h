@@ -11,7 +11,7 @@
 extern "C" {
 #endif
 
-#define KUN_GPU_MODULE_ABI 0x6b470008ull
+#define KUN_GPU_MODULE_ABI 0x6b470009ull
 #define KUN_BLOCK_REGCAP 0x10000
 
 typedef enum { KUN_LAYOUT_STS = 0, KUN_LAYOUT_TS = 1, KUN_LAYOUT_STREAM = 2 } KunGpuLayout;
@@ -41,6 +41,10 @@ typedef struct {
     int64_t length;
     const int32_t *ring_pos;   /* unused */
     void *state;               /* stream mode: the stage's float/double state arrays */
+    /* device word a kernel sets (to 1) when one of its bounded waits for a
+     * bulk copy runs out, instead of hanging; the runtime reads it after a
+     * run (NULL: not reported) */
+    int32_t *error_flag;
     /* stream mode: stocks live in rings of num_stocks (capacity) columns; a
      * launch covers `nseg` segments (sessions): segment k holds stocks
      * [seg_stock0[k], seg_stock0[k] + seg_off[k+1] - seg_off[k]) and is at

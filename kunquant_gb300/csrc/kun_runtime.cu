@@ -262,6 +262,7 @@ static KunStatus enqueue_stages(Executor *ex, const KunGpuModuleDesc *m, const P
         a.total_time = total_time;
         a.start = cur_time;
         a.length = length;
+        a.error_flag = ex->d_error;
         auto tn = ex->tuning.find((const void *)m);
         if (tn != ex->tuning.end() && si < (int)tn->second.size() && !tn->second[si].tile.empty()) {
             a.tune_tile = tn->second[si].tile.data();
@@ -504,6 +505,17 @@ KunStatus run_graph(Executor *ex, const KunGpuModuleDesc *m, const NameMap &name
             set_error("CUDA error: %s", cudaGetErrorString(e));
             return KUN_CUDA_ERROR;
         }
+        if (ex->d_error) {
+            // a kernel whose bounded wait for a bulk copy ran out (never
+            // expected: a hardware or launch-setup fault) reports it here
+            int32_t flag = 0;
+            cudaMemcpy(&flag, ex->d_error, sizeof flag, cudaMemcpyDeviceToHost);
+            if (flag) {
+                cudaMemset(ex->d_error, 0, sizeof(int32_t));
+                set_error("a staged (bulk-copy) kernel timed out waiting for its copies; outputs are not valid");
+                return KUN_CUDA_ERROR;
+            }
+        }
     }
     return KUN_SUCCESS;
 }
@@ -523,6 +535,10 @@ Executor *create_executor(int nstreams) {
         ex->streams.push_back(s);
     }
     ex->epoch = library_epoch();
+    if (cudaMalloc(&ex->d_error, sizeof(int32_t)) == cudaSuccess)
+        cudaMemset(ex->d_error, 0, sizeof(int32_t));
+    else
+        cudaGetLastError();
     return ex;
 }
 
@@ -538,6 +554,7 @@ void destroy_executor(Executor *ex) {
     if (ex->fork) cudaEventDestroy(ex->fork);
     if (ex->bridge_in) cudaEventDestroy(ex->bridge_in);
     if (ex->bridge_out) cudaEventDestroy(ex->bridge_out);
+    if (ex->d_error) cudaFree(ex->d_error);
     for (auto cs : ex->copy_streams) {
         cudaStreamSynchronize(cs);
         cudaStreamDestroy(cs);

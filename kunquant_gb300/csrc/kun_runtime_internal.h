@@ -86,6 +86,7 @@ struct Executor {
     Arena arena;
     Arena staging;
     int64_t last_launches = 0;
+    int32_t *d_error = nullptr;  // set by a kernel whose bounded wait ran out
     uint64_t epoch = 0;  // library_epoch() the module caches below belong to
     std::map<std::tuple<const void *, long long, long long, int>, Plan> plans;
     std::mutex mu;

@@ -495,6 +495,12 @@ class LeveledGen(StageGen):
         # sums, scans in time chunks (see slide.py)
         self.slide = spec.get("form") == "slide"
         self.chunk_mode = False
+        # staged (TMA) instance of an elementwise kernel being generated:
+        # series -> stage index; store_guard keeps threads past the last
+        # stock from storing
+        self.tma_slot: Optional[Dict[int, int]] = None
+        self.store_guard = ""
+        self.tma_kernels: Dict[int, List[str]] = {}
         self.mom: Dict[tuple, str] = {}
         self.cur_level = None
         self.cur_comp: Set[int] = set()
@@ -1127,10 +1133,122 @@ class LeveledGen(StageGen):
             L.append(f"{bi}for (int u = 0; u < {B}; ++u) {name}[u] = n{name[1:]}[u];")
         L.append(f"{ind}}}")
 
+    # ------------------------------------------------------------------ staged (TMA) form
+    def _tma_eligible(self, comp: Set[int], vr: Set[int], wr: Set[int]) -> bool:
+        """An elementwise kernel (no window reads) whose inputs are whole
+        [T][S] series can stage its rows by bulk copies."""
+        ops = self.ops
+        if wr or not vr or len(vr) > 11:
+            return False
+        if any(ops[i]["k"] in ("BackRef", "ForeachBackWindow", "SkipListState") for i in comp):
+            return False
+        for j in vr:
+            op = ops[j]
+            if op.get("single_value"):
+                return False
+            if op["k"] in ("Input", "Output") and self.layout_of(op) != "TS":
+                return False
+        return True
+
+    def _tma_kernel(self, kname: str, pstruct: str, ki: int, comp: Set[int], vr: Set[int], stores: List[int],
+                    loops, decl: List[str], U: int) -> str:
+        """The staged instance of an elementwise kernel: blocks of 128
+        stocks; thread 0 copies kTmaRows rows of every input series into a
+        shared-memory stage with cp.async.bulk (one copy per row: the
+        block's stocks are contiguous), double-buffered on two mbarriers, and
+        the block computes from the stage while the next one is in flight.
+        Waits are bounded: on a time-out the kernel sets the error word and
+        returns instead of hanging."""
+        T = self.T
+        series = sorted(vr)
+        nin = len(series)
+        self.tma_slot = {j: k for k, j in enumerate(series)}
+        self.store_guard = "live && "
+        saved = self.lines
+        self.lines = []
+        self._emit_par_vec(comp, vr, stores, loops, U, "        ")
+        body = self.lines
+        self.lines = saved
+        self.tma_slot = None
+        self.store_guard = ""
+        self.tma_kernels[ki] = [self._series_base(j) for j in series]
+        copies = "\n".join(
+            f"        kun::bulk_copy_g2s(&kst_sm[{k}][b][r][0], (const char*)(b{j} - tid) + (tc + r) * st{j} * "
+            f"(long long)sizeof({T}), rowb, &kst_bar[b]);" for k, j in enumerate(series))
+        return f"""
+__global__ void __launch_bounds__(128) {kname}_tma(const {pstruct} P) {{
+  __shared__ __align__(128) {T} kst_sm[{nin}][2][kun::kTmaRows][128];
+  __shared__ __align__(8) unsigned long long kst_bar[2];
+  const int bx = blockIdx.x, by = blockIdx.y;
+  const int tid = threadIdx.x;
+  const long long S = P.S;
+  const long long s = (long long)bx * 128 + tid;
+  const bool live = s < S;
+  const long long total_time = P.total_time, start = P.start, length = P.length;
+  (void)total_time; (void)start;
+{chr(10).join(decl)}
+  const long long tile = P.tile[{ki}];
+  const long long t0 = (long long)by * tile;
+  const long long t1 = t0 + tile < length ? t0 + tile : length;
+  const long long left = S - (long long)bx * 128;
+  const uint32_t rowb = (uint32_t)((left < 128 ? left : 128) * (long long)sizeof({T}));
+  const int nch = t1 > t0 ? (int)((t1 - t0 + kun::kTmaRows - 1) / kun::kTmaRows) : 0;
+  if (tid == 0) {{
+    kun::mbar_init(&kst_bar[0], 1);
+    kun::mbar_init(&kst_bar[1], 1);
+    kun::mbar_init_fence();
+  }}
+  __syncthreads();
+  auto issue = [&](int c) {{
+    const int b = c & 1;
+    const long long tc = t0 + (long long)c * kun::kTmaRows;
+    const int nr = (int)(t1 - tc < kun::kTmaRows ? t1 - tc : kun::kTmaRows);
+    kun::fence_proxy_async_smem();
+    kun::mbar_arrive_expect_tx(&kst_bar[b], (uint32_t)nr * {nin}u * rowb);
+    for (int r = 0; r < nr; ++r) {{
+{copies}
+    }}
+  }};
+  if (tid == 0 && nch > 0) issue(0);
+  for (int c = 0; c < nch; ++c) {{
+    const int kb = c & 1;
+    if (tid == 0 && c + 1 < nch) issue(c + 1);
+    const bool got = kun::mbar_wait(&kst_bar[kb], (uint32_t)((c >> 1) & 1), kun::kTmaWaitLimit);
+    if (!__syncthreads_and(got)) {{
+      // copies that never completed: report, give those in flight a last
+      // bounded wait (their stage must not be reused), and stop
+      if (tid == 0) {{
+        if (P.err) atomicExch(P.err, 1);
+        kun::mbar_wait(&kst_bar[kb], (uint32_t)((c >> 1) & 1), kun::kTmaWaitLimit);
+        if (c + 1 < nch) kun::mbar_wait(&kst_bar[kb ^ 1], (uint32_t)(((c + 1) >> 1) & 1), kun::kTmaWaitLimit);
+      }}
+      __syncthreads();
+      return;
+    }}
+    const long long tc = t0 + (long long)c * kun::kTmaRows;
+    for (long long t = tc; t < tc + kun::kTmaRows && t < t1; t += {U}) {{
+{chr(10).join(body)}
+    }}
+    __syncthreads();
+  }}
+}}
+"""
+
+    def _series_base(self, j: int) -> str:
+        """Host expression of series j's device base pointer in a launcher."""
+        op = self.ops[j]
+        if op["k"] in ("Input", "Output"):
+            return f"P.p[{self.slot(op['buf'])}]"
+        return f"P.w[{self.scratch[j]}]"
+
     # ------------------------------------------------------------------ vector form
     def _vload(self, j: int, texpr: str) -> str:
         """Read of series j at row `texpr`, NaN outside [0, length); the test
-        is compiled out of the interior instance of the body (KE false)."""
+        is compiled out of the interior instance of the body (KE false).  In
+        the staged instance the row comes from the shared-memory stage."""
+        if self.tma_slot is not None:
+            return (f"(live && ({texpr}) < t1) ? kst_sm[{self.tma_slot[j]}][kb][({texpr}) - tc][tid] "
+                    f": kun::knan<{self.T}>()")
         self.edge_body = True
         return f"kun::ldw<KE>(b{j}, st{j}, (long long)({texpr}), length)"
 
@@ -1166,7 +1284,7 @@ class LeveledGen(StageGen):
                 L.append(f"{ind}{T} v{i}[{U}];")
                 L.append(f"{ind}#pragma unroll")
                 L.append(f"{ind}for (int u = 0; u < {U}; ++u) {{ v{i}[u] = {self.val(a[0])}; "
-                         f"if (t + u < t1) b{i}[(t + u) * st{i}] = v{i}[u]; }}")
+                         f"if ({self.store_guard}t + u < t1) b{i}[(t + u) * st{i}] = v{i}[u]; }}")
             elif k == "ForeachBackWindow":
                 body, reds, own = loops[i]
                 w, seg = op["window"], op.get("segment_end", 0)
@@ -1231,7 +1349,8 @@ class LeveledGen(StageGen):
                 L.append(f"{ind}for (int u = 0; u < {U}; ++u) v{i}[u] = {e};")
         for i in stores:
             L.append(f"{ind}#pragma unroll")
-            L.append(f"{ind}for (int u = 0; u < {U}; ++u) if (t + u < t1) b{i}[(t + u) * st{i}] = {self.val(i)};")
+            L.append(f"{ind}for (int u = 0; u < {U}; ++u) if ({self.store_guard}t + u < t1) "
+                     f"b{i}[(t + u) * st{i}] = {self.val(i)};")
         self.vec = False
 
     def _vstep(self, r: int, ind: str):
@@ -1276,6 +1395,7 @@ class LeveledGen(StageGen):
         for j in mats:
             self.scratch[j] = len(self.scratch)
         srcs, calls, kinfo = [], [], []
+        tma_src: List[str] = []
         knames = []
         pstruct = f"P_{self.kname}"
         for ki, kd in enumerate(ks):
@@ -1330,6 +1450,8 @@ class LeveledGen(StageGen):
                     self.vec_u = U
                 self.lines.append("  }")
                 kinfo.append((chunk, 0))
+                if not (sls or wide) and U == VEC_U_ELEM and self._tma_eligible(comp, vr, wr):
+                    tma_src.append(self._tma_kernel(kname, pstruct, ki, comp, vr, stores, loops, decl, U))
             elif kd["kind"] == "cscan":
                 # one scan role over a time tile of rows, after a warm-up of
                 # its longest window; the tile is a launch parameter like a
@@ -1432,13 +1554,14 @@ struct {pstruct} {{
   void* w[{nscr}];
   long long S, total_time, start, length;
   int tile[{nk}];
+  int* err;
 }};
 """
         self.kernel_info = [(d << 1) | sc for d, sc in kinfo]
         self.num_kernels_override = nk
         # per kernel: time tile (or roles) and block size, from the tuning
         # arrays when given
-        sel = []
+        sel = ["  P.err = a->error_flag;"]
         for k, (d, sc) in enumerate(kinfo):
             sel.append(f"  const int tb{k} = (a->tune_block && a->tune_block[{k}] > 0) ? a->tune_block[{k}] : KUN_TS_THREADS;")
             sel.append(f"  const int blk{k} = tb{k} & 0xffff;")
@@ -1451,13 +1574,21 @@ struct {pstruct} {{
             grid = f"dim3((unsigned)((a->num_stocks + blk{k} - 1) / blk{k}), {gy}), blk{k}, 0, (cudaStream_t)stream"
             if sc:
                 calls.append(f"  {knames[k]}<<<{grid}>>>(P);")
+            elif k in self.tma_kernels:
+                # the staged instance: 128 threads, rows of whole 16-byte
+                # units (S % 4 == 0) from 16-byte aligned series
+                ok = " && ".join([f"kun::aligned16({e})" for e in self.tma_kernels[k]])
+                calls.append(f"  if (kun::tma_enabled() && blk{k} == 128 && (a->num_stocks % 4) == 0 && {ok}) "
+                             f"{knames[k]}_tma<<<{grid}>>>(P);\n"
+                             f"  else if (tb{k} & KUN_BLOCK_REGCAP) {knames[k]}_r<<<{grid}>>>(P);\n"
+                             f"  else {knames[k]}<<<{grid}>>>(P);")
             else:
                 calls.append(f"  if (tb{k} & KUN_BLOCK_REGCAP) {knames[k]}_r<<<{grid}>>>(P);\n"
                              f"  else {knames[k]}<<<{grid}>>>(P);")
             calls.append("  if (cudaError_t e = cudaGetLastError()) return (int)e;")
         launch = self.launcher(pstruct, "\n".join(sel + calls))
         launch += self._group_launcher(pstruct, knames, kinfo)
-        return head + "".join(srcs), launch
+        return head + "".join(srcs) + "".join(tma_src), launch
 
     def _group_launcher(self, pstruct: str, knames: List[str], kinfo) -> str:
         """prepare(): the parameter blocks of n jobs; launch_group(): every
@@ -1508,6 +1639,7 @@ extern "C" size_t {self.kname}_prepare(const KunGpuStageArgs* args, int njobs, v
 {fill}
 {fillw}
       P.S = a->num_stocks; P.total_time = a->total_time; P.start = a->start; P.length = a->length;
+      P.err = a->error_flag;
 {chr(10).join(tiles)}
     }}
   }}
