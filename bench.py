@@ -638,27 +638,12 @@ def main():
     alg_bytes = stage_bytes(spec, top, S, T, elem)
     achieved = alg_bytes / (avg[top] / 1e3) / 1e9
     peak, peak_kind = _peaks()
+    # DRAM traffic of the stage is not measured in this run (an ncu capture
+    # of the same tuned launch shapes would be needed); per-kernel captures
+    # are in profiles/
     traffic = None
-    tf = os.path.join(REPO, "profiles", "traffic.json")
-    if os.path.exists(tf):
-        with open(tf) as f:
-            traffic = json.load(f).get(f"{wl['key']}:{top}")
-    # the same stage against the SM issue rate (one warp instruction per
-    # cycle per scheduler, 4 x 152 schedulers): its kernels' warp
-    # instructions per launch, from ncu, over the measured stage time
-    issue = None
-    inf = os.path.join(REPO, "profiles", "kernel_inst.json")
-    if os.path.exists(inf):
-        with open(inf) as f:
-            inst = json.load(f).get(f"{wl['key']}:{top}")
-        if inst:
-            mhz = (clocks or {}).get("sm_mhz") or 2070.0
-            rate = inst * (S / 5000.0) * (T / 2500.0) / (avg[top] / 1e3) / 1e9
-            peak_i = 4 * 152 * mhz / 1e3
-            issue = {"achieved": rate, "peak": peak_i, "unit": "G warp-inst/s", "frac": rate / peak_i,
-                     "inst_source": "profiles/kernel_inst.json (ncu smsp__inst_executed.sum, scaled to S x T)"}
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind, "issue": issue,
+                "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                 "kernel": f"stage {top} of {wl['key']} ({avg[top]:.3f} ms/launch, "
                           f"{100 * avg[top] / sum(avg.values()):.1f}% of kernel time, single-stream profiled pass)",
                 "whole_step_frac": (wl["n_inputs"] + wl["n_outputs"]) * S * T * elem / (ms_step / 1e3) / 1e9 / peak}
