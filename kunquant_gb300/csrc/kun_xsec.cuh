@@ -429,6 +429,169 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
     __syncthreads();
 }
 
+// Rank of one long row without sorting it: each non-NaN value goes to one
+// of kBucketN buckets by its order-preserving key relative to the row's key
+// range (a monotone map, -0 keyed as +0 so that equal values share a
+// bucket).  From the bucket counts' exclusive scan, a value's rank start is
+// the number of values in lower buckets plus those in its own bucket that
+// are smaller; its end adds the equal ones.  These are exactly the start and
+// end of its equal range in the sorted row (cpp/Kun/Rank.hpp:40-53), so the
+// result is the sort's bit for bit.  Work is O(n) plus the bucket sizes; a
+// row whose largest bucket holds more than kBucketMax values (a narrow or
+// outlier-stretched key range, heavy ties) is left to the radix sort: the
+// function then returns false before writing anything.  Shared memory: the
+// bucketed values over `keys`, counts and fill counters over `counters`.
+constexpr int kBucketLog = 11;
+constexpr int kBucketN = 1 << kBucketLog;
+constexpr int kBucketMax = 48;
+
+template <typename T, int ITEMS>
+__device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T *__restrict__ orow, long long S,
+                                                    typename SortKey<T>::K *keys, uint32_t *counters) {
+    using SK = SortKey<T>;
+    using K = typename SK::K;
+    constexpr int NT = kRankThreads;
+    constexpr int NW = NT / 32;
+    static_assert(kBucketN * 2 <= (NT / 32) * kRadixHistStride, "bucket counters fit the radix counters");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ K red_lo[NW], red_hi[NW];
+    __shared__ int red_n[NW], red_c[NW];
+    __shared__ int scan_w[NW];
+    uint32_t *hist = counters, *fill = counters + kBucketN;
+    T v[ITEMS];
+    K k[ITEMS];
+    int local = 0;
+    K lo = SK::kMax, hi = 0;
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++) {
+        const long long i = (long long)e * NT + tid;
+        v[e] = knan<T>();
+        k[e] = 0;
+        if (i < S) {
+            const T x = row[i];
+            v[e] = x;
+            if (x == x) {
+                k[e] = SK::enc(x == T(0) ? T(0) : x);
+                local++;
+                lo = k[e] < lo ? k[e] : lo;
+                hi = k[e] > hi ? k[e] : hi;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        local += __shfl_xor_sync(0xffffffffu, local, o);
+        const K l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+        lo = l2 < lo ? l2 : lo;
+        hi = h2 > hi ? h2 : hi;
+    }
+    if (lane == 0) {
+        red_n[warp] = local;
+        red_lo[warp] = lo;
+        red_hi[warp] = hi;
+    }
+    for (int b = tid; b < 2 * kBucketN; b += NT) counters[b] = 0;
+    __syncthreads();
+    int n = 0;
+    lo = SK::kMax;
+    hi = 0;
+    for (int w = 0; w < NW; w++) {
+        n += red_n[w];
+        lo = red_lo[w] < lo ? red_lo[w] : lo;
+        hi = red_hi[w] > hi ? red_hi[w] : hi;
+    }
+    if (n > 0) {
+        const K range = hi - lo;
+        int bits = 0;
+        while (bits < (int)(sizeof(K) * 8) && (range >> bits) != 0) bits++;
+        const int shift = bits > kBucketLog ? bits - kBucketLog : 0;
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++)
+            if (v[e] == v[e]) atomicAdd(&hist[(int)((k[e] - lo) >> shift)], 1u);
+        __syncthreads();
+        // the largest bucket decides: buckets or the radix sort
+        int mc = 0;
+        for (int b = tid; b < kBucketN; b += NT) mc = max(mc, (int)hist[b]);
+        for (int o = 16; o > 0; o >>= 1) mc = max(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+        if (lane == 0) red_c[warp] = mc;
+        __syncthreads();
+        mc = 0;
+        for (int w = 0; w < NW; w++) mc = max(mc, red_c[w]);
+        if (mc > kBucketMax) {
+            __syncthreads();
+            return false;
+        }
+        // exclusive scan of the counts (kBucketN / NT per thread, in order)
+        constexpr int PER = kBucketN / NT;
+        uint32_t c[PER], sum = 0;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            c[j] = hist[tid * PER + j];
+            sum += c[j];
+        }
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) scan_w[warp] = (int)incl;
+        __syncthreads();
+        if (tid < 32) {
+            int x = tid < NW ? scan_w[tid] : 0;
+            const int v0 = x;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (tid >= o) x += y;
+            }
+            if (tid < NW) scan_w[tid] = x - v0;
+        }
+        __syncthreads();
+        uint32_t run = (uint32_t)scan_w[warp] + incl - sum;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            hist[tid * PER + j] = run;
+            run += c[j];
+        }
+        __syncthreads();
+        // the values by bucket (unordered inside a bucket)
+        T *vals = reinterpret_cast<T *>(keys);
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++)
+            if (v[e] == v[e]) {
+                const int b = (int)((k[e] - lo) >> shift);
+                vals[hist[b] + atomicAdd(&fill[b], 1u)] = v[e];
+            }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) {
+            const long long i = (long long)e * NT + tid;
+            if (i >= S) continue;
+            T res = knan<T>();
+            if (v[e] == v[e]) {
+                const int b = (int)((k[e] - lo) >> shift);
+                const int p0 = (int)hist[b], p1 = b + 1 < kBucketN ? (int)hist[b + 1] : n;
+                long long less = p0, eq = 0;
+                for (int p = p0; p < p1; p++) {
+                    const T y = vals[p];
+                    less += (y < v[e]);
+                    eq += (y == v[e]);
+                }
+                const long long start = less, end = less + eq;
+                const long long rsum = (start + end + 1) * (end - start) / 2;
+                res = kdiv(kdiv((T)rsum, (T)(end - start)), (T)n);
+            }
+            orow[i] = res;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) {
+            const long long i = (long long)e * NT + tid;
+            if (i < S) orow[i] = knan<T>();
+        }
+    }
+    __syncthreads();
+    return true;
+}
+
 // shared memory of a rank block sorting up to P keys
 template <typename T>
 inline size_t rank_smem_bytes(int P) {
@@ -449,10 +612,12 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ 
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
     for (long long t = blockIdx.x; t < length; t += gridDim.x) {
-        if (P >= kRadixMinP)
-            rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, idx, cnt_warp);
-        else
+        if (P >= kRadixMinP) {
+            if (!rank_one_row_bucket<T, ITEMS>(in + t * S, out + t * S, S, keys, counters))
+                rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, idx, cnt_warp);
+        } else {
             rank_one_row<T, ITEMS>(in + t * S, out + t * S, S, P, keys, cnt_warp);
+        }
     }
 }
 
@@ -475,10 +640,12 @@ __global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restric
     K *keys = reinterpret_cast<K *>(smem_raw);
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
-    if (Pk >= kRadixMinP)
-        rank_one_row_radix<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys, counters,
-                                     idx, cnt_warp);
-    else
+    if (Pk >= kRadixMinP) {
+        if (!rank_one_row_bucket<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys,
+                                           counters))
+            rank_one_row_radix<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys,
+                                         counters, idx, cnt_warp);
+    } else
         rank_one_row<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, Pk, keys, cnt_warp);
 }
 
@@ -520,9 +687,10 @@ __global__ void __launch_bounds__(SMALL ? kRankSmallThreads : kRankThreads)
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
     if (SMALL)
         rank_one_row<T, ITEMS>(in, out, len, Pk, keys, cnt_warp);
-    else if (Pk >= kRadixMinP)
-        rank_one_row_radix<T, ITEMS>(in, out, len, keys, counters, idx, cnt_warp);
-    else
+    else if (Pk >= kRadixMinP) {
+        if (!rank_one_row_bucket<T, ITEMS>(in, out, len, keys, counters))
+            rank_one_row_radix<T, ITEMS>(in, out, len, keys, counters, idx, cnt_warp);
+    } else
         rank_one_row<T, ITEMS>(in, out, len, Pk, keys, cnt_warp);
 }
 
@@ -714,10 +882,12 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows_multi(const RankRowsJo
         T *out = (T *)jb.out + t * S;
         int Pk = ITEMS;
         while (Pk < S) Pk <<= 1;
-        if (Pk >= kRadixMinP)
-            rank_one_row_radix<T, ITEMS>(in, out, S, keys, counters, idx, cnt_warp);
-        else
+        if (Pk >= kRadixMinP) {
+            if (!rank_one_row_bucket<T, ITEMS>(in, out, S, keys, counters))
+                rank_one_row_radix<T, ITEMS>(in, out, S, keys, counters, idx, cnt_warp);
+        } else {
             rank_one_row<T, ITEMS>(in, out, S, Pk, keys, cnt_warp);
+        }
     }
 }
 

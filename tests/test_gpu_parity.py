@@ -98,8 +98,9 @@ def test_multistream_graph_replay_bit_exact():
                                        ("rank_ties_nan", 8192), ("rank_ties_nan", 9000),
                                        ("rank2_exact", 3000), ("rank029_f64", 3000)])
 def test_rank_long_rows_bit_exact(fixture, S):
-    """Rows long enough for the radix-sort rank (and the wider 16-key form
-    above 8192 stocks), with ties, +-0 and NaN rows, against the oracle."""
+    """Rows long enough for the bucketed rank or, when a bucket overflows,
+    the radix-sort rank (and the wider 16-key form above 8192 stocks), with
+    ties, +-0 and NaN rows, against the oracle."""
     from kunquant_gb300 import build
     from tests import golden_util as G
     spec = G.load(fixture)[0]
@@ -112,6 +113,15 @@ def test_rank_long_rows_bit_exact(fixture, S):
     a[7, :] = 0.0
     a[7, ::2] = -0.0
     a[9] = rng.random(S).astype(dt)                              # no ties
+    # rows for the bucketed rank: spread values with a few ties, +-0 and NaN
+    a[11] = rng.normal(0, 1, S).astype(dt)
+    a[11, 1::5] = a[11, ::5][:len(a[11, 1::5])]
+    a[11, ::97] = np.nan
+    a[11, 10], a[11, 20], a[11, 30] = 0.0, -0.0, 0.0
+    a[13] = rng.random(S).astype(dt)
+    a[13, 17] = 1e30                                             # stretched range
+    a[15] = np.exp(rng.uniform(-20, 20, S)).astype(dt)           # many binades
+    a[15, ::7] = a[15, 3]
     key = "units_" + fixture
     if key not in _libs:
         _libs[key] = kr.Library.load(build.build_module_library([spec], "kun_rank_" + fixture))
