@@ -430,17 +430,21 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
 }
 
 // Rank of one long row without sorting it: each non-NaN value goes to one
-// of kBucketN buckets by its order-preserving key relative to the row's key
-// range (a monotone map, -0 keyed as +0 so that equal values share a
-// bucket).  From the bucket counts' exclusive scan, a value's rank start is
-// the number of values in lower buckets plus those in its own bucket that
-// are smaller; its end adds the equal ones.  These are exactly the start and
-// end of its equal range in the sorted row (cpp/Kun/Rank.hpp:40-53), so the
-// result is the sort's bit for bit.  Work is O(n) plus the bucket sizes; a
-// row whose largest bucket holds more than kBucketMax values (a narrow or
-// outlier-stretched key range, heavy ties) is left to the radix sort: the
-// function then returns false before writing anything.  Shared memory: the
-// bucketed values over `keys`, counts and fill counters over `counters`.
+// of kBucketN buckets by a monotone map of its value, and from the bucket
+// counts' exclusive scan a value's rank start is the number of values in
+// lower buckets plus those in its own bucket that are smaller; its end adds
+// the equal ones.  These are exactly the start and end of its equal range in
+// the sorted row (cpp/Kun/Rank.hpp:40-53), so the result is the sort's bit
+// for bit.  Two maps are counted and the one with the smaller largest bucket
+// is used: linear in the value (floor((x - min) * scale), monotone because
+// each rounded step is) for values spread evenly, and linear in the
+// order-preserving key (logarithmic in the value; -0 keyed as +0 so equal
+// values share a bucket) for values spread over many binades.  Work is O(n)
+// plus the bucket sizes; a row whose largest bucket under both maps holds
+// more than kBucketMax values (heavy ties, outliers) is left to the radix
+// sort: the function then returns false before writing anything.  Shared
+// memory: the bucketed values over `keys`, the two maps' counts and the fill
+// counters over `counters`.
 constexpr int kBucketLog = 11;
 constexpr int kBucketN = 1 << kBucketLog;
 constexpr int kBucketMax = 48;
@@ -452,16 +456,18 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
     using K = typename SK::K;
     constexpr int NT = kRankThreads;
     constexpr int NW = NT / 32;
-    static_assert(kBucketN * 2 <= (NT / 32) * kRadixHistStride, "bucket counters fit the radix counters");
+    static_assert(kBucketN * 3 <= (NT / 32) * kRadixHistStride, "bucket counters fit the radix counters");
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     __shared__ K red_lo[NW], red_hi[NW];
-    __shared__ int red_n[NW], red_c[NW];
+    __shared__ T red_vlo[NW], red_vhi[NW];
+    __shared__ int red_n[NW], red_c[NW], red_c2[NW];
     __shared__ int scan_w[NW];
-    uint32_t *hist = counters, *fill = counters + kBucketN;
+    uint32_t *hist_v = counters, *hist_k = counters + kBucketN, *fill = counters + 2 * kBucketN;
     T v[ITEMS];
     K k[ITEMS];
     int local = 0;
     K lo = SK::kMax, hi = 0;
+    T vlo = kinf<T>(), vhi = -kinf<T>();
 #pragma unroll
     for (int e = 0; e < ITEMS; e++) {
         const long long i = (long long)e * NT + tid;
@@ -475,6 +481,8 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
                 local++;
                 lo = k[e] < lo ? k[e] : lo;
                 hi = k[e] > hi ? k[e] : hi;
+                vlo = x < vlo ? x : vlo;
+                vhi = x > vhi ? x : vhi;
             }
         }
     }
@@ -483,43 +491,81 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
         const K l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
         lo = l2 < lo ? l2 : lo;
         hi = h2 > hi ? h2 : hi;
+        const T vl2 = __shfl_xor_sync(0xffffffffu, vlo, o), vh2 = __shfl_xor_sync(0xffffffffu, vhi, o);
+        vlo = vl2 < vlo ? vl2 : vlo;
+        vhi = vh2 > vhi ? vh2 : vhi;
     }
     if (lane == 0) {
         red_n[warp] = local;
         red_lo[warp] = lo;
         red_hi[warp] = hi;
+        red_vlo[warp] = vlo;
+        red_vhi[warp] = vhi;
     }
-    for (int b = tid; b < 2 * kBucketN; b += NT) counters[b] = 0;
+    for (int b = tid; b < 3 * kBucketN; b += NT) counters[b] = 0;
     __syncthreads();
     int n = 0;
     lo = SK::kMax;
     hi = 0;
+    vlo = kinf<T>();
+    vhi = -kinf<T>();
     for (int w = 0; w < NW; w++) {
         n += red_n[w];
         lo = red_lo[w] < lo ? red_lo[w] : lo;
         hi = red_hi[w] > hi ? red_hi[w] : hi;
+        vlo = red_vlo[w] < vlo ? red_vlo[w] : vlo;
+        vhi = red_vhi[w] > vhi ? red_vhi[w] : vhi;
     }
     if (n > 0) {
         const K range = hi - lo;
         int bits = 0;
         while (bits < (int)(sizeof(K) * 8) && (range >> bits) != 0) bits++;
         const int shift = bits > kBucketLog ? bits - kBucketLog : 0;
+        // linear map: scale so that the largest value lands in the last
+        // bucket (a non-finite or zero spread puts every value in bucket 0)
+        const T spread = vhi - vlo;
+        const T scale = (spread > T(0) && spread < kinf<T>()) ? T(kBucketN - 1) / spread : T(0);
+        auto bucket_v = [&](T x) {
+            const T f = (x - vlo) * scale;
+            const int b = f >= T(kBucketN - 1) ? kBucketN - 1 : (f > T(0) ? (int)f : 0);
+            return b;
+        };
+        auto bucket_k = [&](K key) { return (int)((key - lo) >> shift); };
 #pragma unroll
         for (int e = 0; e < ITEMS; e++)
-            if (v[e] == v[e]) atomicAdd(&hist[(int)((k[e] - lo) >> shift)], 1u);
+            if (v[e] == v[e]) {
+                atomicAdd(&hist_v[bucket_v(v[e])], 1u);
+                atomicAdd(&hist_k[bucket_k(k[e])], 1u);
+            }
         __syncthreads();
-        // the largest bucket decides: buckets or the radix sort
-        int mc = 0;
-        for (int b = tid; b < kBucketN; b += NT) mc = max(mc, (int)hist[b]);
-        for (int o = 16; o > 0; o >>= 1) mc = max(mc, __shfl_xor_sync(0xffffffffu, mc, o));
-        if (lane == 0) red_c[warp] = mc;
+        // the map with the smaller largest bucket; the radix sort if both
+        // overflow
+        int mv = 0, mk = 0;
+        for (int b = tid; b < kBucketN; b += NT) {
+            mv = max(mv, (int)hist_v[b]);
+            mk = max(mk, (int)hist_k[b]);
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            mv = max(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+            mk = max(mk, __shfl_xor_sync(0xffffffffu, mk, o));
+        }
+        if (lane == 0) {
+            red_c[warp] = mv;
+            red_c2[warp] = mk;
+        }
         __syncthreads();
-        mc = 0;
-        for (int w = 0; w < NW; w++) mc = max(mc, red_c[w]);
-        if (mc > kBucketMax) {
+        mv = 0;
+        mk = 0;
+        for (int w = 0; w < NW; w++) {
+            mv = max(mv, red_c[w]);
+            mk = max(mk, red_c2[w]);
+        }
+        if (mv > kBucketMax && mk > kBucketMax) {
             __syncthreads();
             return false;
         }
+        const bool lin = mv <= mk;
+        uint32_t *hist = lin ? hist_v : hist_k;
         // exclusive scan of the counts (kBucketN / NT per thread, in order)
         constexpr int PER = kBucketN / NT;
         uint32_t c[PER], sum = 0;
@@ -554,12 +600,15 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
         __syncthreads();
         // the values by bucket (unordered inside a bucket)
         T *vals = reinterpret_cast<T *>(keys);
+        int bk[ITEMS];
 #pragma unroll
-        for (int e = 0; e < ITEMS; e++)
+        for (int e = 0; e < ITEMS; e++) {
+            bk[e] = 0;
             if (v[e] == v[e]) {
-                const int b = (int)((k[e] - lo) >> shift);
-                vals[hist[b] + atomicAdd(&fill[b], 1u)] = v[e];
+                bk[e] = lin ? bucket_v(v[e]) : bucket_k(k[e]);
+                vals[hist[bk[e]] + atomicAdd(&fill[bk[e]], 1u)] = v[e];
             }
+        }
         __syncthreads();
 #pragma unroll
         for (int e = 0; e < ITEMS; e++) {
@@ -567,7 +616,7 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
             if (i >= S) continue;
             T res = knan<T>();
             if (v[e] == v[e]) {
-                const int b = (int)((k[e] - lo) >> shift);
+                const int b = bk[e];
                 const int p0 = (int)hist[b], p1 = b + 1 < kBucketN ? (int)hist[b + 1] : n;
                 long long less = p0, eq = 0;
                 for (int p = p0; p < p1; p++) {
