@@ -280,7 +280,9 @@ def serving(nsess=256, rate=20000.0, seconds=3.0, warm=250, seed=3):
                 inflight[j] = pending[j].popleft()
             pool.submit_all([sess[j] for j in batch])
     el = time.perf_counter() - t0
-    _, steps = pool.take_latencies()
+    # the pool's own record: submit to result, per tick (without the
+    # harness's arrival queue and polling)
+    native, steps = pool.take_latencies()
     pool.shutdown()
     lat = np.asarray(lat) * 1e6
     # the same kind of tick through one StreamContext per session, one call after another
@@ -303,6 +305,8 @@ def serving(nsess=256, rate=20000.0, seconds=3.0, warm=250, seed=3):
             "p99_tick_us": float(np.percentile(lat, 99)), "session_ticks_per_s": lat.size / el,
             "stock_ticks_per_s": float(lat.size / el * sizes.mean()),
             "mean_sessions_per_step": float(np.mean(steps)) if len(steps) else None,
+            "pool_submit_to_result_us": {"p50": float(np.percentile(native, 50)) if len(native) else None,
+                                         "p99": float(np.percentile(native, 99)) if len(native) else None},
             "pool_bytes": serve.pool_bytes(mod, cap),
             "one_context_per_session": {"ms_per_session_tick": per_call * 1e3,
                                         "max_session_ticks_per_s": 1.0 / per_call}}
