@@ -42,6 +42,9 @@ template <> struct SortKey<double> {
 };
 
 constexpr int kRankThreads = 1024;
+// dynamic shared memory above which a launch first raises the kernel's
+// limit: 48 KB less room for the kernels' static arrays
+constexpr size_t kSmemOptIn = 40 * 1024;
 constexpr int kRadixMinP = 2048;  // rows at least this long (padded) use the radix sort
 __host__ __device__ inline int skew(int p) { return p + (p >> 5); }
 // keys per thread for a sort of P keys by kRankThreads threads
@@ -929,7 +932,7 @@ inline int launch_rank_items(const T *in, T *out, long long S, long long length,
     const size_t bsmem = rank_bucket_smem<T>(S);
     const bool bucket = P >= kRadixMinP && bsmem <= 227 * 1024;
     if (bucket) {
-        if (bsmem > 48 * 1024) {
+        if (bsmem > kSmemOptIn) {
             cudaError_t e =
                 cudaFuncSetAttribute(rank_rows_bucket<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
             if (e != cudaSuccess) return (int)e;
@@ -938,7 +941,7 @@ inline int launch_rank_items(const T *in, T *out, long long S, long long length,
         if (cudaError_t e = cudaGetLastError()) return (int)e;
     }
     size_t smem = rank_smem_bytes<T>(P);
-    if (smem > 48 * 1024) {
+    if (smem > kSmemOptIn) {
         cudaError_t e =
             cudaFuncSetAttribute(rank_rows<T, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
@@ -1024,7 +1027,7 @@ inline int launch_rank_rows_multi(const RankRowsJob *d_jobs, int njobs, long lon
     const size_t bsmem = rank_bucket_smem<T>(max_S);
     const bool bucket = P >= kRadixMinP && bsmem <= 227 * 1024;
     if (bucket) {
-        if (bsmem > 48 * 1024) {
+        if (bsmem > kSmemOptIn) {
             cudaError_t e = cudaFuncSetAttribute(rank_rows_multi_bucket<T>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
             if (e != cudaSuccess) return (int)e;
@@ -1033,7 +1036,7 @@ inline int launch_rank_rows_multi(const RankRowsJob *d_jobs, int njobs, long lon
         if (cudaError_t e = cudaGetLastError()) return (int)e;
     }
     auto go = [&](auto kernel, bool marked_only) {
-        if (smem > 48 * 1024) {
+        if (smem > kSmemOptIn) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return (int)e;
         }
@@ -1063,7 +1066,7 @@ template <typename T>
 inline int launch_scale(const T *in, T *out, long long S, long long length, cudaStream_t st) {
     size_t smem = (size_t)S * sizeof(T);
     if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
-    if (smem > 48 * 1024) {
+    if (smem > kSmemOptIn) {
         cudaError_t e = cudaFuncSetAttribute(scale_rows<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
@@ -1088,7 +1091,7 @@ inline int launch_rank_segments(const T *in, int w_in, T *out, int w_out, long l
     size_t smem = rank_smem_bytes<T>(P);
     if (smem > 227 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
     auto go = [&](auto kernel) {
-        if (smem > 48 * 1024) {
+        if (smem > kSmemOptIn) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return (int)e;
         }
@@ -1131,7 +1134,7 @@ inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long lon
     const size_t bsmem = rank_bucket_smem<T>(P);
     const bool bucket = bsmem <= 227 * 1024;
     if (bucket) {
-        if (bsmem > 48 * 1024) {
+        if (bsmem > kSmemOptIn) {
             cudaError_t e = cudaFuncSetAttribute(rank_multi_segments_bucket<T>,
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
             if (e != cudaSuccess) return (int)e;
@@ -1141,7 +1144,7 @@ inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long lon
         if (cudaError_t e = cudaGetLastError()) return (int)e;
     }
     auto go = [&](auto kernel) {
-        if (smem > 48 * 1024) {
+        if (smem > kSmemOptIn) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return (int)e;
         }
@@ -1161,7 +1164,7 @@ inline int launch_scale_segments(const T *in, int w_in, T *out, int w_out, long 
                                  const int32_t *cnt, cudaStream_t st) {
     size_t smem = (size_t)max_len * sizeof(T);
     if (smem > 200 * 1024) return (int)cudaErrorInvalidValue;
-    if (smem > 48 * 1024) {
+    if (smem > kSmemOptIn) {
         cudaError_t e = cudaFuncSetAttribute(scale_segments<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
