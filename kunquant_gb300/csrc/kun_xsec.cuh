@@ -443,64 +443,50 @@ __device__ __forceinline__ void rank_one_row_radix(const T *__restrict__ row, T 
 // each rounded step is) for values spread evenly, and linear in the
 // order-preserving key (logarithmic in the value; -0 keyed as +0 so equal
 // values share a bucket) for values spread over many binades.  Work is O(n)
-// plus the bucket sizes.  The row lives in shared memory, not registers, so
-// the kernels that use this run two 1024-thread blocks (two rows) per SM.
-// A row whose largest bucket under both maps holds more than kBucketMax
-// values (heavy ties, outliers) is not ranked here: its first output gets
-// the RankMark payload and a radix-sort launch after this one ranks exactly
-// the marked rows.
+// plus the bucket sizes; a row whose largest bucket under both maps holds
+// more than kBucketMax values (heavy ties, outliers) is left to the radix
+// sort: the function then returns false before writing anything.  Shared
+// memory: the bucketed values over `keys`, the two maps' counts and the fill
+// counters over `counters`.
 constexpr int kBucketLog = 11;
 constexpr int kBucketN = 1 << kBucketLog;
 constexpr int kBucketMax = 48;
 
-// a NaN payload no rank output carries (they write the quiet NaN or numbers)
-template <typename T> struct RankMark;
-template <> struct RankMark<float> {
-    static __device__ __forceinline__ void set(float *p) { *p = __uint_as_float(0x7fbadbadu); }
-    static __device__ __forceinline__ bool is(const float *p) { return __float_as_uint(*p) == 0x7fbadbadu; }
-};
-template <> struct RankMark<double> {
-    static __device__ __forceinline__ void set(double *p) {
-        *p = __longlong_as_double((long long)0x7ff4badbadbadbadull);
-    }
-    static __device__ __forceinline__ bool is(const double *p) {
-        return (unsigned long long)__double_as_longlong(*p) == 0x7ff4badbadbadbadull;
-    }
-};
-
-// shared memory of a bucket-rank block for rows of at most S values
-template <typename T>
-__host__ __device__ inline size_t rank_bucket_smem(long long S) {
-    return 2 * (((size_t)S * sizeof(T) + 15) / 16 * 16) + 3 * (size_t)kBucketN * sizeof(uint32_t);
-}
-
-template <typename T>
-__device__ __forceinline__ bool rank_bucket_row(const T *__restrict__ row, T *__restrict__ orow, long long S,
-                                                unsigned char *smem, long long S_cap) {
+template <typename T, int ITEMS>
+__device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T *__restrict__ orow, long long S,
+                                                    typename SortKey<T>::K *keys, uint32_t *counters) {
     using SK = SortKey<T>;
     using K = typename SK::K;
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, NT = blockDim.x, NW = NT >> 5;
-    const size_t row_bytes = ((size_t)S_cap * sizeof(T) + 15) / 16 * 16;
-    T *xs = reinterpret_cast<T *>(smem);
-    T *vals = reinterpret_cast<T *>(smem + row_bytes);
-    uint32_t *hist_v = reinterpret_cast<uint32_t *>(smem + 2 * row_bytes);
-    uint32_t *hist_k = hist_v + kBucketN, *fill = hist_v + 2 * kBucketN;
-    __shared__ K red_lo[32], red_hi[32];
-    __shared__ T red_vlo[32], red_vhi[32];
-    __shared__ int red_n[32], red_c[32], red_c2[32], scan_w[32];
+    constexpr int NT = kRankThreads;
+    constexpr int NW = NT / 32;
+    static_assert(kBucketN * 3 <= (NT / 32) * kRadixHistStride, "bucket counters fit the radix counters");
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    __shared__ K red_lo[NW], red_hi[NW];
+    __shared__ T red_vlo[NW], red_vhi[NW];
+    __shared__ int red_n[NW], red_c[NW], red_c2[NW];
+    __shared__ int scan_w[NW];
+    uint32_t *hist_v = counters, *hist_k = counters + kBucketN, *fill = counters + 2 * kBucketN;
+    T v[ITEMS];
+    K k[ITEMS];
     int local = 0;
     K lo = SK::kMax, hi = 0;
     T vlo = kinf<T>(), vhi = -kinf<T>();
-    for (long long i = tid; i < S; i += NT) {
-        const T x = row[i];
-        xs[i] = x;
-        if (x == x) {
-            const K k = SK::enc(x == T(0) ? T(0) : x);
-            local++;
-            lo = k < lo ? k : lo;
-            hi = k > hi ? k : hi;
-            vlo = x < vlo ? x : vlo;
-            vhi = x > vhi ? x : vhi;
+#pragma unroll
+    for (int e = 0; e < ITEMS; e++) {
+        const long long i = (long long)e * NT + tid;
+        v[e] = knan<T>();
+        k[e] = 0;
+        if (i < S) {
+            const T x = row[i];
+            v[e] = x;
+            if (x == x) {
+                k[e] = SK::enc(x == T(0) ? T(0) : x);
+                local++;
+                lo = k[e] < lo ? k[e] : lo;
+                hi = k[e] > hi ? k[e] : hi;
+                vlo = x < vlo ? x : vlo;
+                vhi = x > vhi ? x : vhi;
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -519,7 +505,7 @@ __device__ __forceinline__ bool rank_bucket_row(const T *__restrict__ row, T *__
         red_vlo[warp] = vlo;
         red_vhi[warp] = vhi;
     }
-    for (int b = tid; b < 3 * kBucketN; b += NT) hist_v[b] = 0;
+    for (int b = tid; b < 3 * kBucketN; b += NT) counters[b] = 0;
     __syncthreads();
     int n = 0;
     lo = SK::kMax;
@@ -533,128 +519,129 @@ __device__ __forceinline__ bool rank_bucket_row(const T *__restrict__ row, T *__
         vlo = red_vlo[w] < vlo ? red_vlo[w] : vlo;
         vhi = red_vhi[w] > vhi ? red_vhi[w] : vhi;
     }
-    if (n == 0) {
-        for (long long i = tid; i < S; i += NT) orow[i] = knan<T>();
-        __syncthreads();
-        return true;
-    }
-    const K range = hi - lo;
-    int bits = 0;
-    while (bits < (int)(sizeof(K) * 8) && (range >> bits) != 0) bits++;
-    const int shift = bits > kBucketLog ? bits - kBucketLog : 0;
-    // linear map: the largest value lands in the last bucket (a non-finite
-    // or zero spread puts every value in bucket 0)
-    const T spread = vhi - vlo;
-    const T scale = (spread > T(0) && spread < kinf<T>()) ? T(kBucketN - 1) / spread : T(0);
-    auto bucket_v = [&](T x) {
-        const T f = (x - vlo) * scale;
-        return f >= T(kBucketN - 1) ? kBucketN - 1 : (f > T(0) ? (int)f : 0);
-    };
-    auto bucket_k = [&](T x) { return (int)((SK::enc(x == T(0) ? T(0) : x) - lo) >> shift); };
-    for (long long i = tid; i < S; i += NT) {
-        const T x = xs[i];
-        if (x == x) {
-            atomicAdd(&hist_v[bucket_v(x)], 1u);
-            atomicAdd(&hist_k[bucket_k(x)], 1u);
-        }
-    }
-    __syncthreads();
-    // the map with the smaller largest bucket; marked for the radix sort if
-    // both overflow
-    int mv = 0, mk = 0;
-    for (int b = tid; b < kBucketN; b += NT) {
-        mv = max(mv, (int)hist_v[b]);
-        mk = max(mk, (int)hist_k[b]);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        mv = max(mv, __shfl_xor_sync(0xffffffffu, mv, o));
-        mk = max(mk, __shfl_xor_sync(0xffffffffu, mk, o));
-    }
-    if (lane == 0) {
-        red_c[warp] = mv;
-        red_c2[warp] = mk;
-    }
-    __syncthreads();
-    mv = 0;
-    mk = 0;
-    for (int w = 0; w < NW; w++) {
-        mv = max(mv, red_c[w]);
-        mk = max(mk, red_c2[w]);
-    }
-    if (mv > kBucketMax && mk > kBucketMax) {
-        if (tid == 0) RankMark<T>::set(orow);
-        __syncthreads();
-        return false;
-    }
-    const bool lin = mv <= mk;
-    uint32_t *hist = lin ? hist_v : hist_k;
-    // exclusive scan of the counts, kBucketN / NT consecutive ones a thread
-    const int per = kBucketN / NT;
-    uint32_t sum = 0;
-    for (int j = 0; j < per; j++) sum += hist[tid * per + j];
-    uint32_t incl = sum;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    if (lane == 31) scan_w[warp] = (int)incl;
-    __syncthreads();
-    if (tid < 32) {
-        int x = tid < NW ? scan_w[tid] : 0;
-        const int x0 = x;
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, x, o);
-            if (tid >= o) x += y;
-        }
-        if (tid < NW) scan_w[tid] = x - x0;
-    }
-    __syncthreads();
-    uint32_t run = (uint32_t)scan_w[warp] + incl - sum;
-    for (int j = 0; j < per; j++) {
-        const uint32_t c = hist[tid * per + j];
-        hist[tid * per + j] = run;
-        run += c;
-    }
-    __syncthreads();
-    // the values by bucket (unordered inside a bucket)
-    for (long long i = tid; i < S; i += NT) {
-        const T x = xs[i];
-        if (x == x) {
-            const int b = lin ? bucket_v(x) : bucket_k(x);
-            vals[hist[b] + atomicAdd(&fill[b], 1u)] = x;
-        }
-    }
-    __syncthreads();
-    for (long long i = tid; i < S; i += NT) {
-        const T x = xs[i];
-        T res = knan<T>();
-        if (x == x) {
-            const int b = lin ? bucket_v(x) : bucket_k(x);
-            const int p0 = (int)hist[b], p1 = b + 1 < kBucketN ? (int)hist[b + 1] : n;
-            long long less = p0, eq = 0;
-            for (int p = p0; p < p1; p++) {
-                const T y = vals[p];
-                less += (y < x);
-                eq += (y == x);
+    if (n > 0) {
+        const K range = hi - lo;
+        int bits = 0;
+        while (bits < (int)(sizeof(K) * 8) && (range >> bits) != 0) bits++;
+        const int shift = bits > kBucketLog ? bits - kBucketLog : 0;
+        // linear map: scale so that the largest value lands in the last
+        // bucket (a non-finite or zero spread puts every value in bucket 0)
+        const T spread = vhi - vlo;
+        const T scale = (spread > T(0) && spread < kinf<T>()) ? T(kBucketN - 1) / spread : T(0);
+        auto bucket_v = [&](T x) {
+            const T f = (x - vlo) * scale;
+            const int b = f >= T(kBucketN - 1) ? kBucketN - 1 : (f > T(0) ? (int)f : 0);
+            return b;
+        };
+        auto bucket_k = [&](K key) { return (int)((key - lo) >> shift); };
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++)
+            if (v[e] == v[e]) {
+                atomicAdd(&hist_v[bucket_v(v[e])], 1u);
+                atomicAdd(&hist_k[bucket_k(k[e])], 1u);
             }
-            const long long start = less, end = less + eq;
-            const long long rsum = (start + end + 1) * (end - start) / 2;
-            res = kdiv(kdiv((T)rsum, (T)(end - start)), (T)n);
+        __syncthreads();
+        // the map with the smaller largest bucket; the radix sort if both
+        // overflow
+        int mv = 0, mk = 0;
+        for (int b = tid; b < kBucketN; b += NT) {
+            mv = max(mv, (int)hist_v[b]);
+            mk = max(mk, (int)hist_k[b]);
         }
-        orow[i] = res;
+        for (int o = 16; o > 0; o >>= 1) {
+            mv = max(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+            mk = max(mk, __shfl_xor_sync(0xffffffffu, mk, o));
+        }
+        if (lane == 0) {
+            red_c[warp] = mv;
+            red_c2[warp] = mk;
+        }
+        __syncthreads();
+        mv = 0;
+        mk = 0;
+        for (int w = 0; w < NW; w++) {
+            mv = max(mv, red_c[w]);
+            mk = max(mk, red_c2[w]);
+        }
+        if (mv > kBucketMax && mk > kBucketMax) {
+            __syncthreads();
+            return false;
+        }
+        const bool lin = mv <= mk;
+        uint32_t *hist = lin ? hist_v : hist_k;
+        // exclusive scan of the counts (kBucketN / NT per thread, in order)
+        constexpr int PER = kBucketN / NT;
+        uint32_t c[PER], sum = 0;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            c[j] = hist[tid * PER + j];
+            sum += c[j];
+        }
+        uint32_t incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) scan_w[warp] = (int)incl;
+        __syncthreads();
+        if (tid < 32) {
+            int x = tid < NW ? scan_w[tid] : 0;
+            const int v0 = x;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xffffffffu, x, o);
+                if (tid >= o) x += y;
+            }
+            if (tid < NW) scan_w[tid] = x - v0;
+        }
+        __syncthreads();
+        uint32_t run = (uint32_t)scan_w[warp] + incl - sum;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            hist[tid * PER + j] = run;
+            run += c[j];
+        }
+        __syncthreads();
+        // the values by bucket (unordered inside a bucket)
+        T *vals = reinterpret_cast<T *>(keys);
+        int bk[ITEMS];
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) {
+            bk[e] = 0;
+            if (v[e] == v[e]) {
+                bk[e] = lin ? bucket_v(v[e]) : bucket_k(k[e]);
+                vals[hist[bk[e]] + atomicAdd(&fill[bk[e]], 1u)] = v[e];
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) {
+            const long long i = (long long)e * NT + tid;
+            if (i >= S) continue;
+            T res = knan<T>();
+            if (v[e] == v[e]) {
+                const int b = bk[e];
+                const int p0 = (int)hist[b], p1 = b + 1 < kBucketN ? (int)hist[b + 1] : n;
+                long long less = p0, eq = 0;
+                for (int p = p0; p < p1; p++) {
+                    const T y = vals[p];
+                    less += (y < v[e]);
+                    eq += (y == v[e]);
+                }
+                const long long start = less, end = less + eq;
+                const long long rsum = (start + end + 1) * (end - start) / 2;
+                res = kdiv(kdiv((T)rsum, (T)(end - start)), (T)n);
+            }
+            orow[i] = res;
+        }
+    } else {
+#pragma unroll
+        for (int e = 0; e < ITEMS; e++) {
+            const long long i = (long long)e * NT + tid;
+            if (i < S) orow[i] = knan<T>();
+        }
     }
     __syncthreads();
     return true;
-}
-
-// whether this block should rank the row at `orow` in a marked-only launch
-template <typename T>
-__device__ __forceinline__ bool rank_row_marked(const T *orow) {
-    __shared__ int marked;
-    __syncthreads();
-    if (threadIdx.x == 0) marked = RankMark<T>::is(orow) ? 1 : 0;
-    __syncthreads();
-    return marked != 0;
 }
 
 // shared memory of a rank block sorting up to P keys
@@ -669,7 +656,7 @@ inline size_t rank_smem_bytes(int P) {
 
 template <typename T, int ITEMS>
 __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ in, T *__restrict__ out,
-                                                          long long S, long long length, int P, bool marked_only) {
+                                                          long long S, long long length, int P) {
     using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
@@ -677,21 +664,13 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows(const T *__restrict__ 
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
     for (long long t = blockIdx.x; t < length; t += gridDim.x) {
-        if (marked_only && !rank_row_marked(out + t * S)) continue;
-        if (P >= kRadixMinP)
-            rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, idx, cnt_warp);
-        else
+        if (P >= kRadixMinP) {
+            if (!rank_one_row_bucket<T, ITEMS>(in + t * S, out + t * S, S, keys, counters))
+                rank_one_row_radix<T, ITEMS>(in + t * S, out + t * S, S, keys, counters, idx, cnt_warp);
+        } else {
             rank_one_row<T, ITEMS>(in + t * S, out + t * S, S, P, keys, cnt_warp);
+        }
     }
-}
-
-// the bucket rank over rows (two 1024-thread blocks an SM)
-template <typename T>
-__global__ void __launch_bounds__(kRankThreads, 2) rank_rows_bucket(const T *__restrict__ in, T *__restrict__ out,
-                                                                    long long S, long long length) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    for (long long t = blockIdx.x; t < length; t += gridDim.x)
-        rank_bucket_row<T>(in + t * S, out + t * S, S, smem_raw, S);
 }
 
 // stream mode: one block per segment, each at its own ring row
@@ -713,10 +692,12 @@ __global__ void __launch_bounds__(kRankThreads) rank_segments(const T *__restric
     K *keys = reinterpret_cast<K *>(smem_raw);
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
-    if (Pk >= kRadixMinP)
-        rank_one_row_radix<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys, counters,
-                                     idx, cnt_warp);
-    else
+    if (Pk >= kRadixMinP) {
+        if (!rank_one_row_bucket<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys,
+                                           counters))
+            rank_one_row_radix<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, keys,
+                                         counters, idx, cnt_warp);
+    } else
         rank_one_row<T, ITEMS>(in + (n % w_in) * cap + s0, out + (n % w_out) * cap + s0, len, Pk, keys, cnt_warp);
 }
 
@@ -740,8 +721,7 @@ constexpr int kRankSmallThreads = kRankSmallMax / 8;
 template <typename T, int ITEMS, bool SMALL>
 __global__ void __launch_bounds__(SMALL ? kRankSmallThreads : kRankThreads)
     rank_multi_segments(const RankJob *__restrict__ jobs, long long cap, const int32_t *seg_off,
-                        const int32_t *seg_stock0, const long long *seg_tick, int P, const int32_t *cnt,
-                        bool marked_only) {
+                        const int32_t *seg_stock0, const long long *seg_tick, int P, const int32_t *cnt) {
     using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
@@ -757,29 +737,13 @@ __global__ void __launch_bounds__(SMALL ? kRankSmallThreads : kRankThreads)
     K *keys = reinterpret_cast<K *>(smem_raw);
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
-    if (marked_only && Pk >= kRadixMinP && !rank_row_marked(out)) return;
     if (SMALL)
         rank_one_row<T, ITEMS>(in, out, len, Pk, keys, cnt_warp);
-    else if (Pk >= kRadixMinP)
-        rank_one_row_radix<T, ITEMS>(in, out, len, keys, counters, idx, cnt_warp);
-    else
+    else if (Pk >= kRadixMinP) {
+        if (!rank_one_row_bucket<T, ITEMS>(in, out, len, keys, counters))
+            rank_one_row_radix<T, ITEMS>(in, out, len, keys, counters, idx, cnt_warp);
+    } else
         rank_one_row<T, ITEMS>(in, out, len, Pk, keys, cnt_warp);
-}
-
-// the bucket rank of the long segments (k >= cnt[3], or every segment
-// without a table), two 1024-thread blocks an SM
-template <typename T>
-__global__ void __launch_bounds__(kRankThreads, 2)
-    rank_multi_segments_bucket(const RankJob *__restrict__ jobs, long long cap, const int32_t *seg_off,
-                               const int32_t *seg_stock0, const long long *seg_tick, int P, const int32_t *cnt) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int k = blockIdx.x;
-    if (cnt && (k >= cnt[0] || k < cnt[3])) return;
-    const RankJob jb = jobs[blockIdx.y];
-    const long long len = seg_off[k + 1] - seg_off[k], s0 = seg_stock0[k], n = seg_tick[k];
-    if (len > P || len <= kRankSmallMax) return;
-    rank_bucket_row<T>((const T *)jb.in + (n % jb.w_in) * cap + s0, (T *)jb.out + (n % jb.w_out) * cap + s0, len,
-                       smem_raw, P);
 }
 
 template <typename T>
@@ -927,26 +891,14 @@ inline int kun_num_sms() {
 
 template <typename T, int ITEMS>
 inline int launch_rank_items(const T *in, T *out, long long S, long long length, int P, cudaStream_t st) {
-    long long grid = length < (long long)kun_num_sms() * 2 ? length : (long long)kun_num_sms() * 2;
-    // long rows: the bucket rank first, then the radix sort of the rows it marked
-    const size_t bsmem = rank_bucket_smem<T>(S);
-    const bool bucket = P >= kRadixMinP && bsmem <= 227 * 1024;
-    if (bucket) {
-        if (bsmem > kSmemOptIn) {
-            cudaError_t e =
-                cudaFuncSetAttribute(rank_rows_bucket<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
-            if (e != cudaSuccess) return (int)e;
-        }
-        rank_rows_bucket<T><<<(unsigned)grid, kRankThreads, bsmem, st>>>(in, out, S, length);
-        if (cudaError_t e = cudaGetLastError()) return (int)e;
-    }
     size_t smem = rank_smem_bytes<T>(P);
     if (smem > kSmemOptIn) {
         cudaError_t e =
             cudaFuncSetAttribute(rank_rows<T, ITEMS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return (int)e;
     }
-    rank_rows<T, ITEMS><<<(unsigned)grid, kRankThreads, smem, st>>>(in, out, S, length, P, bucket);
+    long long grid = length < (long long)kun_num_sms() * 2 ? length : (long long)kun_num_sms() * 2;
+    rank_rows<T, ITEMS><<<(unsigned)grid, kRankThreads, smem, st>>>(in, out, S, length, P);
     return (int)cudaGetLastError();
 }
 
@@ -959,19 +911,9 @@ struct RankRowsJob {
     long long S, length, row0;
 };
 
-__device__ __forceinline__ int rank_rows_job(const RankRowsJob *__restrict__ jobs, int njobs, long long r) {
-    int lo = 0, hi = njobs - 1;  // the job whose rows hold r
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (jobs[mid].row0 <= r) lo = mid;
-        else hi = mid - 1;
-    }
-    return lo;
-}
-
 template <typename T, int ITEMS>
 __global__ void __launch_bounds__(kRankThreads) rank_rows_multi(const RankRowsJob *__restrict__ jobs, int njobs,
-                                                                long long total_rows, int P, bool marked_only) {
+                                                                long long total_rows, int P) {
     using K = typename SortKey<T>::K;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ int cnt_warp[kRankThreads / 32];
@@ -979,7 +921,13 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows_multi(const RankRowsJo
     uint32_t *counters = reinterpret_cast<uint32_t *>(smem_raw + ((size_t)rank_key_slots(P) * sizeof(K) + 15) / 16 * 16);
     uint16_t *idx = reinterpret_cast<uint16_t *>(counters + radix_hist_slots());
     for (long long r = blockIdx.x; r < total_rows; r += gridDim.x) {
-        const RankRowsJob jb = jobs[rank_rows_job(jobs, njobs, r)];
+        int lo = 0, hi = njobs - 1;  // the job whose rows hold r
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (jobs[mid].row0 <= r) lo = mid;
+            else hi = mid - 1;
+        }
+        const RankRowsJob jb = jobs[lo];
         const long long t = r - jb.row0, S = jb.S;
         if (t < 0 || t >= jb.length || S <= 0 || S > P) continue;
         const T *in = (const T *)jb.in + t * S;
@@ -987,27 +935,11 @@ __global__ void __launch_bounds__(kRankThreads) rank_rows_multi(const RankRowsJo
         int Pk = ITEMS;
         while (Pk < S) Pk <<= 1;
         if (Pk >= kRadixMinP) {
-            // long rows: only those the bucket rank marked, when it ran
-            if (marked_only && !rank_row_marked(out)) continue;
-            rank_one_row_radix<T, ITEMS>(in, out, S, keys, counters, idx, cnt_warp);
+            if (!rank_one_row_bucket<T, ITEMS>(in, out, S, keys, counters))
+                rank_one_row_radix<T, ITEMS>(in, out, S, keys, counters, idx, cnt_warp);
         } else {
             rank_one_row<T, ITEMS>(in, out, S, Pk, keys, cnt_warp);
         }
-    }
-}
-
-// the bucket rank of the jobs' rows of at least kRadixMinP / 2 + 1 stocks
-// (the rows the radix sort would take)
-template <typename T>
-__global__ void __launch_bounds__(kRankThreads, 2) rank_rows_multi_bucket(const RankRowsJob *__restrict__ jobs,
-                                                                          int njobs, long long total_rows,
-                                                                          long long S_cap) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    for (long long r = blockIdx.x; r < total_rows; r += gridDim.x) {
-        const RankRowsJob jb = jobs[rank_rows_job(jobs, njobs, r)];
-        const long long t = r - jb.row0, S = jb.S;
-        if (t < 0 || t >= jb.length || S <= kRadixMinP / 2 || S > S_cap) continue;
-        rank_bucket_row<T>((const T *)jb.in + t * S, (T *)jb.out + t * S, S, smem_raw, S_cap);
     }
 }
 
@@ -1022,31 +954,18 @@ inline int launch_rank_rows_multi(const RankRowsJob *d_jobs, int njobs, long lon
     const size_t smem = rank_smem_bytes<T>(P);
     if (smem > 227 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
     const long long grid = total_rows < (long long)kun_num_sms() * 2 ? total_rows : (long long)kun_num_sms() * 2;
-    // long rows: the bucket rank first, then the radix sort of the rows it
-    // marked (and the short rows' bitonic sort in the same launch)
-    const size_t bsmem = rank_bucket_smem<T>(max_S);
-    const bool bucket = P >= kRadixMinP && bsmem <= 227 * 1024;
-    if (bucket) {
-        if (bsmem > kSmemOptIn) {
-            cudaError_t e = cudaFuncSetAttribute(rank_rows_multi_bucket<T>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
-            if (e != cudaSuccess) return (int)e;
-        }
-        rank_rows_multi_bucket<T><<<(unsigned)grid, kRankThreads, bsmem, st>>>(d_jobs, njobs, total_rows, max_S);
-        if (cudaError_t e = cudaGetLastError()) return (int)e;
-    }
-    auto go = [&](auto kernel, bool marked_only) {
+    auto go = [&](auto kernel) {
         if (smem > kSmemOptIn) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return (int)e;
         }
-        kernel<<<(unsigned)grid, kRankThreads, smem, st>>>(d_jobs, njobs, total_rows, P, marked_only);
+        kernel<<<(unsigned)grid, kRankThreads, smem, st>>>(d_jobs, njobs, total_rows, P);
         return (int)cudaGetLastError();
     };
     switch (rank_items(P)) {
-    case 8: return go(rank_rows_multi<T, 8>, bucket);
-    case 16: return go(rank_rows_multi<T, 16>, bucket);
-    default: return go(rank_rows_multi<T, 32>, bucket);
+    case 8: return go(rank_rows_multi<T, 8>);
+    case 16: return go(rank_rows_multi<T, 16>);
+    default: return go(rank_rows_multi<T, 32>);
     }
 }
 
@@ -1121,7 +1040,7 @@ inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long lon
     if (cnt || max_len <= kRankSmallMax) {
         const size_t smem = rank_smem_bytes<T>(kRankSmallMax);
         rank_multi_segments<T, 8, true><<<grid, kRankSmallThreads, smem, st>>>(d_jobs, cap, seg_off, seg_stock0,
-                                                                            seg_tick, kRankSmallMax, cnt, false);
+                                                                            seg_tick, kRankSmallMax, cnt);
         if (cudaError_t e = cudaGetLastError()) return (int)e;
     }
     if (!cnt && max_len <= kRankSmallMax) return 0;
@@ -1130,25 +1049,12 @@ inline int launch_rank_multi_segments(const RankJob *d_jobs, int njobs, long lon
     while (P < max_len) P <<= 1;
     size_t smem = rank_smem_bytes<T>(P);
     if (smem > 227 * 1024 || P > 32 * kRankThreads) return (int)cudaErrorInvalidValue;
-    // the bucket rank first, then the radix sort of the segments it marked
-    const size_t bsmem = rank_bucket_smem<T>(P);
-    const bool bucket = bsmem <= 227 * 1024;
-    if (bucket) {
-        if (bsmem > kSmemOptIn) {
-            cudaError_t e = cudaFuncSetAttribute(rank_multi_segments_bucket<T>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bsmem);
-            if (e != cudaSuccess) return (int)e;
-        }
-        rank_multi_segments_bucket<T><<<grid, kRankThreads, bsmem, st>>>(d_jobs, cap, seg_off, seg_stock0, seg_tick,
-                                                                          P, cnt);
-        if (cudaError_t e = cudaGetLastError()) return (int)e;
-    }
     auto go = [&](auto kernel) {
         if (smem > kSmemOptIn) {
             cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return (int)e;
         }
-        kernel<<<grid, kRankThreads, smem, st>>>(d_jobs, cap, seg_off, seg_stock0, seg_tick, P, cnt, bucket);
+        kernel<<<grid, kRankThreads, smem, st>>>(d_jobs, cap, seg_off, seg_stock0, seg_tick, P, cnt);
         return (int)cudaGetLastError();
     };
     switch (rank_items(P)) {
