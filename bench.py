@@ -691,14 +691,19 @@ def main():
         host_in = {k: torch.from_numpy(v).pin_memory().numpy() for k, v in data.items()}
         host_out = {n: torch.empty((T, S), dtype=torch.float32).pin_memory().numpy()
                     for n in mod.getOutputNames()}
-        kr.runGraph(ex, mod, host_in, 0, T, outputs=host_out)
+        for _ in range(max(1, args.warmup)):
+            kr.runGraph(ex, mod, host_in, 0, T, outputs=host_out)
+        step_ms = []
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            ts = time.perf_counter()
             kr.runGraph(ex, mod, host_in, 0, T, outputs=host_out)
+            step_ms.append((time.perf_counter() - ts) * 1e3)
         dt = (time.perf_counter() - t0) / args.steps
         e2e = {"value": world * S * T / dt, "unit": "stock-days/s",
                "h2d_bytes_per_step": wl["n_inputs"] * S * T * elem,
-               "d2h_bytes_per_step": len(host_out) * S * T * elem, "ms_per_step": dt * 1e3}
+               "d2h_bytes_per_step": len(host_out) * S * T * elem, "ms_per_step": dt * 1e3,
+               "step_ms_median": float(np.median(step_ms)), "step_ms_max": max(step_ms)}
     serve_line = None
     if rank == 0 and not args.no_serve:
         serve_line = serving()
