@@ -547,7 +547,17 @@ template <typename T, int W> struct LinReg {
 // the outputs are formed from those sums without the cancellation of fp32.
 template <int W> struct SlideLinReg {
     float isum = 0, xsum = 0, x2sum = 0;
+    // The value sums are taken about an origin c, the first non-NaN value the
+    // state sees, with each difference y - c kept exactly as a pair.  The
+    // state starts empty and a value leaves the window only after it entered
+    // it, so every value is added and taken out about the same origin.  The
+    // variance N*sum(d^2) - sum(d)^2 of a window of nearly equal values then
+    // cancels at the level of their spread, not of their price (two closes
+    // 1e-5 apart at 327 would otherwise lose ~1e10 x 2^-48 of it); slope,
+    // R^2 and the residual do not depend on the origin.
     DFloat ysum, y2sum, xysum;
+    float c = 0.f;
+    bool has_c = false;
     int nn = W;
     template <bool SharedSq>
     __device__ __forceinline__ void step(float old, float cur) {
@@ -556,19 +566,30 @@ template <int W> struct SlideLinReg {
         x2sum = __fsub_rn(__fadd_rn(x2sum, isum), __fmul_rn(2.f, xsum));
         xsum = __fsub_rn(xsum, isum);
         const bool on = old != old, cn = cur != cur;
+        if (!cn && !has_c) {
+            c = cur;  // nothing has been added yet, so no old value is pending
+            has_c = true;
+        }
         if (!on) {
+            const DFloat d = df_two_sum(old, -c);
             isum = __fsub_rn(isum, 1.f);
-            df_acc(ysum, -old);
-            df_acc_prod_neg(y2sum, old, old);
+            df_acc(ysum, -d.hi);
+            ysum.lo = __fsub_rn(ysum.lo, d.lo);
+            df_acc_prod_neg(y2sum, d.hi, d.hi);
+            y2sum.lo = __fmaf_rn(-2.f * d.hi, d.lo, y2sum.lo);
         }
         nn = nn - (int)on + (int)cn;
         if (!cn) {
+            const DFloat d = df_two_sum(cur, -c);
             isum = __fadd_rn(isum, 1.f);
             xsum = __fadd_rn(xsum, w);
             x2sum = __fadd_rn(x2sum, w * w);
-            df_acc(ysum, cur);
-            df_acc_prod(y2sum, cur, cur);
-            df_acc_prod(xysum, w, cur);
+            df_acc(ysum, d.hi);
+            ysum.lo = __fadd_rn(ysum.lo, d.lo);
+            df_acc_prod(y2sum, d.hi, d.hi);
+            y2sum.lo = __fmaf_rn(2.f * d.hi, d.lo, y2sum.lo);
+            df_acc_prod(xysum, w, d.hi);
+            xysum.lo = __fmaf_rn(w, d.lo, xysum.lo);
         }
     }
     __device__ __forceinline__ float n() const { return (float)(W - nn); }
@@ -577,7 +598,7 @@ template <int W> struct SlideLinReg {
         const float N = n();
         DFloat a = df_scale(xysum, N);
         df_acc_pair(a, df_scale(ysum, -xsum));
-        return df_fast_two_sum(a.hi, a.lo);
+        return df_two_sum(a.hi, a.lo);  // hi may have cancelled below lo
     }
     // N*x2sum - xsum*xsum: exact in float
     __device__ __forceinline__ float varx() const {
@@ -585,20 +606,22 @@ template <int W> struct SlideLinReg {
     }
     __device__ __forceinline__ float rsq() const {
         const float N = n();
-        const DFloat ys = df_fast_two_sum(ysum.hi, ysum.lo);
+        const DFloat ys = df_two_sum(ysum.hi, ysum.lo);
         DFloat vy = df_scale(y2sum, N);
         df_acc_pair(vy, -kmul(ys, ys));
         const float r = (float)cov();
         return __fdiv_rn(__fmul_rn(r, r), __fmul_rn(varx(), (float)vy));
     }
     __device__ __forceinline__ float slope() const { return __fdiv_rn((float)cov(), varx()); }
-    // val - (slope*W + ym - slope*xm) = (N*val - ysum - slope*(W*N - xsum)) / N,
+    // val - (slope*W + ym - slope*xm) = (N*(val-c) - ysum - slope*(W*N - xsum)) / N,
     // with the slope kept as a pair: the residual is a small difference of
     // large terms
     __device__ __forceinline__ float resi(float val) const {
         const float N = n();
         const DFloat sd = kdiv(cov(), DFloat(varx()));
-        DFloat r = df_prod(N, val);
+        const DFloat dv = df_two_sum(val, -c);
+        DFloat r = df_prod(N, dv.hi);
+        r.lo = __fmaf_rn(N, dv.lo, r.lo);
         df_acc_pair(r, -ysum);
         df_acc_pair(r, -kmul(sd, DFloat(__fsub_rn(__fmul_rn((float)W, N), xsum))));
         return __fdiv_rn((float)r, N);

@@ -96,3 +96,25 @@ def test_alpha158_slide_benchmarked_size():
                 bad_med.append((k, float(rel.median())))
     assert not bad_nan, bad_nan
     assert not bad_med, bad_med
+
+
+@pytest.mark.gpu
+def test_alpha158_slide_regression_near_equal_prices():
+    """Prices log-uniform in [1, 1e5], and every 16th stock's second close
+    set 1e-5 (relative) from its first: the two-row regression windows at the
+    start then have a variance ~1e10 times below the square of their sum.
+    Every BETA/RSQR/RESI cell stays within 1e-5 of fp64 (R^2 of two rows is
+    exactly 1)."""
+    S, T = 256, 300
+    d32 = synth.ohlcv(S, T, seed=77, nan_frac=0.0, price_range=(1.0, 1e5))
+    close = d32["close"]
+    for s in range(0, S, 16):
+        close[1, s] = np.float32(close[0, s] * (1.0 + 1e-5))
+    want = OracleProgram(predefined_spec("alpha158_f64")).run({k: v.astype(np.float64) for k, v in d32.items()})
+    ex = kr.createSingleThreadExecutor()
+    got = kr.runGraph(ex, kr.Library.predefined("alpha158_slide_f32").getModule("alpha158_slide"), d32, 0, T)
+    st = _errors(got, want)
+    reg = [f for f in st if f.startswith(("BETA", "RSQR", "RESI"))]
+    assert len(reg) == 15
+    assert all(st[f][0] <= 1e-5 and st[f][2] == 0 for f in reg), {f: st[f] for f in reg if st[f][0] > 1e-5}
+    assert np.all(np.abs(np.asarray(got["RSQR5"])[1, ::16] - 1.0) <= 1e-5)
