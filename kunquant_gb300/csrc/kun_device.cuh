@@ -416,6 +416,50 @@ template <typename T, bool IsMax> struct RArg {
     }
     __device__ __forceinline__ T value() const { return idx; }
 };
+// The same Min/Max/ArgMin/ArgMax of a window taken in runs of positions, so
+// that rows whose windows overlap share the run they have in common.  A state
+// covers one run; then(b) continues it with a later run b and gives exactly
+// the state that stepping through both runs in order gives: NaN in either run
+// is NaN; Min/Max keep the later of equal values as kmin/kmax do; Arg keeps
+// the earlier position of equal values, as only a strictly better value
+// replaces it.  Positions are small integers relative to the row tile, held
+// in T.
+template <typename T, bool IsMax, bool IsArg> struct RExt {
+    T v = IsMax ? -kinf<T>() : kinf<T>();
+    T pos = 0;
+    __device__ __forceinline__ void step(T x, T p) {
+        const bool isn = kisnan(v) || kisnan(x);
+        if (IsArg) {
+            const bool cmp = IsMax ? (v < x) : (v > x);
+            v = cmp ? x : v;
+            pos = cmp ? p : pos;
+        } else {
+            v = IsMax ? kmax(v, x) : kmin(v, x);
+        }
+        v = isn ? knan<T>() : v;
+    }
+    __device__ __forceinline__ void then(const RExt &b) {
+        const bool isn = kisnan(v) || kisnan(b.v);
+        if (IsArg) {
+            const bool cmp = IsMax ? (v < b.v) : (v > b.v);
+            v = cmp ? b.v : v;
+            pos = cmp ? b.pos : pos;
+        } else {
+            v = IsMax ? kmax(v, b.v) : kmin(v, b.v);
+        }
+        v = isn ? knan<T>() : v;
+    }
+    // RArg's index of the window ending at `row`: the distance back to the
+    // chosen position, 0 when no value beat the starting infinity
+    __device__ __forceinline__ T arg(T row) const {
+        if (kisnan(v)) return knan<T>();
+        return v == (IsMax ? -kinf<T>() : kinf<T>()) ? T(0) : ksub(row, pos);
+    }
+};
+template <typename T> struct RVal {
+    T v;
+    __device__ __forceinline__ T value() const { return v; }
+};
 template <typename T> struct RRank {
     T v, less = 0, eq = 0;
     __device__ __forceinline__ RRank() {}

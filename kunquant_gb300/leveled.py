@@ -1285,6 +1285,9 @@ __global__ void __launch_bounds__(128) {kname}_tma(const {pstruct} P) {{
                 L.append(f"{ind}#pragma unroll")
                 L.append(f"{ind}for (int u = 0; u < {U}; ++u) {{ v{i}[u] = {self.val(a[0])}; "
                          f"if ({self.store_guard}t + u < t1) b{i}[(t + u) * st{i}] = v{i}[u]; }}")
+            elif k == "ForeachBackWindow" and self._ext_chain(self.plan.loop_chain[i], loops, U):
+                if i == chain_head[i]:
+                    self._emit_ext_chain(self.plan.loop_chain[i], loops, U, ind)
             elif k == "ForeachBackWindow":
                 body, reds, own = loops[i]
                 w, seg = op["window"], op.get("segment_end", 0)
@@ -1352,6 +1355,90 @@ __global__ void __launch_bounds__(128) {kname}_tma(const {pstruct} P) {{
             L.append(f"{ind}for (int u = 0; u < {U}; ++u) if ({self.store_guard}t + u < t1) "
                      f"b{i}[(t + u) * st{i}] = {self.val(i)};")
         self.vec = False
+
+    EXT_KINDS = {"ReduceMax": ("true", "false"), "ReduceMin": ("false", "false"),
+                 "ReduceArgMax": ("true", "true"), "ReduceArgMin": ("false", "true")}
+
+    def _ext_chain(self, chain: List[int], loops, U: int) -> bool:
+        """A loop chain whose reductions are all Min/Max/ArgMin/ArgMax of a
+        window value, over windows of at least U rows that all end at the
+        row: the U rows of a step then share all but U-1 positions of each
+        window (kun::RExt)."""
+        ops = self.ops
+        reds = loops[chain[-1]][1]
+        if not reds or any(ops[r]["k"] not in self.EXT_KINDS for r in reds):
+            return False
+        if any(ops[ops[r]["in"][0]]["k"] != "IterValue" for r in reds):
+            return False
+        for a, b in zip(chain, chain[1:]):
+            if ops[a].get("segment_end", 0) != ops[b]["window"]:
+                return False
+        if ops[chain[-1]].get("segment_end", 0) != 0:
+            return False
+        return all(ops[l]["window"] >= U for l in chain)
+
+    def _emit_ext_chain(self, chain: List[int], loops, U: int, ind: str):
+        """The U rows t..t+U-1 of a window of w rows: row u covers positions
+        t+u-w+1 .. t+u.  Positions t+U-w .. t are common to all U rows and are
+        stepped once (kun::RExt, longest window first, each window's state
+        joining at its first position); each row then steps its older edge
+        (t+u-w+1 .. t+U-1-w), continues with the common run and steps its
+        newer edge (t+1 .. t+u).  In position order, as the loop would."""
+        ops, T, L = self.ops, self.T, self.lines
+        reds = loops[chain[-1]][1]
+        win = {r: ops[contraction.reduction_loop(ops, r)]["window"] for r in reds}
+        src = {r: ops[ops[r]["in"][0]]["in"][1] for r in reds}
+        kind = {r: self.EXT_KINDS[ops[r]["k"]] for r in reds}
+
+        def ext(r):
+            mx, arg = kind[r]
+            return f"kun::RExt<{T}, {mx}, {arg}>"
+
+        for r in reds:
+            L.append(f"{ind}kun::RVal<{T}> r{r}[{U}];")
+        L.append(f"{ind}{{")
+        bi = ind + "  "
+        for r in reds:
+            L.append(f"{bi}{ext(r)} c{r};")
+        ws = sorted(set(win.values()), reverse=True)
+        for n, w in enumerate(ws):
+            hi, lo = w - U, (ws[n + 1] - U + 1 if n + 1 < len(ws) else 0)
+            if hi < lo:
+                continue
+            active = [r for r in reds if win[r] >= w]
+            L.append(f"{bi}#pragma unroll {VEC_UNROLL}")
+            L.append(f"{bi}for (int d = {hi}; d >= {lo}; --d) {{")
+            for s in sorted({src[r] for r in active}):
+                L.append(f"{bi}  const {T} x{s} = {self._vload(s, 't - d')};")
+            for r in active:
+                L.append(f"{bi}  c{r}.step(x{src[r]}, ({T})(-d));")
+            L.append(f"{bi}}}")
+        # the edge rows: o{s}_{w}[k] = row t+1-w+k, n{s}[k] = row t+1+k (k < U-1)
+        for s, w in sorted({(src[r], win[r]) for r in reds}):
+            L.append(f"{bi}{T} o{s}_{w}[{U - 1}];")
+            L.append(f"{bi}#pragma unroll")
+            L.append(f"{bi}for (int k = 0; k < {U - 1}; ++k) o{s}_{w}[k] = {self._vload(s, f't + 1 - {w} + k')};")
+        for s in sorted(set(src.values())):
+            L.append(f"{bi}{T} n{s}[{U - 1}];")
+            L.append(f"{bi}#pragma unroll")
+            L.append(f"{bi}for (int k = 0; k < {U - 1}; ++k) n{s}[k] = {self._vload(s, 't + 1 + k')};")
+        L.append(f"{bi}#pragma unroll")
+        L.append(f"{bi}for (int u = 0; u < {U}; ++u) {{")
+        bj = bi + "  "
+        for r in reds:
+            s, w = src[r], win[r]
+            L.append(f"{bj}{{")
+            L.append(f"{bj}  {ext(r)} a;")
+            L.append(f"{bj}  #pragma unroll")
+            L.append(f"{bj}  for (int k = u; k < {U - 1}; ++k) a.step(o{s}_{w}[k], ({T})(k + 1 - {w}));")
+            L.append(f"{bj}  a.then(c{r});")
+            L.append(f"{bj}  #pragma unroll")
+            L.append(f"{bj}  for (int k = 0; k < u; ++k) a.step(n{s}[k], ({T})(k + 1));")
+            res = f"a.arg(({T})u)" if kind[r][1] == "true" else "a.v"
+            L.append(f"{bj}  r{r}[u].v = {res};")
+            L.append(f"{bj}}}")
+        L.append(f"{bi}}}")
+        L.append(f"{ind}}}")
 
     def _vstep(self, r: int, ind: str):
         """Per-lane reduction step inside the lane loop."""

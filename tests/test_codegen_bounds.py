@@ -16,10 +16,13 @@ from kunquant_gb300.graph import predefined_spec
 
 READ = re.compile(r"kun::ldw<KE>\(b\d+, st\d+, \(long long\)\(([^)]*)\), length\)")
 LOOP = re.compile(r"for \(int iter = (\d+); iter >= (\d+); --iter\)")
+# the shared run of a window extreme (kun::RExt): d counts down, row t - d
+DLOOP = re.compile(r"for \(int d = (\d+); d >= (\d+); --d\)")
 
 
-def _offsets(expr, U, loop):
-    """(min, max) of expr - t."""
+def _offsets(expr, U, loop, dloop=None):
+    """(min, max) of expr - t.  The edge rows of a window extreme are read
+    for k < U - 1."""
     m = re.fullmatch(r"t \+ u", expr)
     if m:
         return 0, U - 1
@@ -33,6 +36,15 @@ def _offsets(expr, U, loop):
         n = int(m.group(1))
         a, b = loop
         return n - a, n - b
+    if expr == "t - d":
+        assert dloop is not None, expr
+        return -dloop[0], -dloop[1]
+    m = re.fullmatch(r"t \+ 1 - (\d+) \+ k", expr)
+    if m:
+        w = int(m.group(1))
+        return 1 - w, U - 1 - w
+    if expr == "t + 1 + k":
+        return 1, U - 1
     raise AssertionError(f"unrecognised row expression: {expr}")
 
 
@@ -60,7 +72,9 @@ def test_interior_reads_stay_in_bounds(key, tmp_path):
         for r in READ.finditer(text):
             loops = [l for l in LOOP.finditer(text, 0, r.start())]
             loop = (int(loops[-1].group(1)), int(loops[-1].group(2))) if loops else None
-            lo, hi = _offsets(r.group(1), U, loop)
+            dloops = [l for l in DLOOP.finditer(text, 0, r.start())]
+            dloop = (int(dloops[-1].group(1)), int(dloops[-1].group(2))) if dloops else None
+            lo, hi = _offsets(r.group(1), U, loop, dloop)
             assert -lo <= wmax, f"{name}: reads t{lo:+d}, interior needs t0 >= {-lo}, has {wmax}"
             assert hi - U <= fwd - 1, f"{name}: reads t+{hi} with t <= t1 - {U}, interior has t1 + {fwd} <= length"
             checked += 1
