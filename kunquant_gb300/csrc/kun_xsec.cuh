@@ -507,18 +507,36 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
     }
     for (int b = tid; b < 3 * kBucketN; b += NT) counters[b] = 0;
     __syncthreads();
-    int n = 0;
-    lo = SK::kMax;
-    hi = 0;
-    vlo = kinf<T>();
-    vhi = -kinf<T>();
-    for (int w = 0; w < NW; w++) {
-        n += red_n[w];
-        lo = red_lo[w] < lo ? red_lo[w] : lo;
-        hi = red_hi[w] > hi ? red_hi[w] : hi;
-        vlo = red_vlo[w] < vlo ? red_vlo[w] : vlo;
-        vhi = red_vhi[w] > vhi ? red_vhi[w] : vhi;
+    // warp 0 combines the warps' partials and leaves the row's in slot 0
+    if (warp == 0) {
+        local = lane < NW ? red_n[lane] : 0;
+        lo = lane < NW ? red_lo[lane] : SK::kMax;
+        hi = lane < NW ? red_hi[lane] : K(0);
+        vlo = lane < NW ? red_vlo[lane] : kinf<T>();
+        vhi = lane < NW ? red_vhi[lane] : -kinf<T>();
+        for (int o = 16; o > 0; o >>= 1) {
+            local += __shfl_xor_sync(0xffffffffu, local, o);
+            const K l2 = __shfl_xor_sync(0xffffffffu, lo, o), h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+            lo = l2 < lo ? l2 : lo;
+            hi = h2 > hi ? h2 : hi;
+            const T vl2 = __shfl_xor_sync(0xffffffffu, vlo, o), vh2 = __shfl_xor_sync(0xffffffffu, vhi, o);
+            vlo = vl2 < vlo ? vl2 : vlo;
+            vhi = vh2 > vhi ? vh2 : vhi;
+        }
+        if (lane == 0) {
+            red_n[0] = local;
+            red_lo[0] = lo;
+            red_hi[0] = hi;
+            red_vlo[0] = vlo;
+            red_vhi[0] = vhi;
+        }
     }
+    __syncthreads();
+    const int n = red_n[0];
+    lo = red_lo[0];
+    hi = red_hi[0];
+    vlo = red_vlo[0];
+    vhi = red_vhi[0];
     if (n > 0) {
         const K range = hi - lo;
         int bits = 0;
@@ -557,12 +575,21 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
             red_c2[warp] = mk;
         }
         __syncthreads();
-        mv = 0;
-        mk = 0;
-        for (int w = 0; w < NW; w++) {
-            mv = max(mv, red_c[w]);
-            mk = max(mk, red_c2[w]);
+        if (warp == 0) {
+            mv = lane < NW ? red_c[lane] : 0;
+            mk = lane < NW ? red_c2[lane] : 0;
+            for (int o = 16; o > 0; o >>= 1) {
+                mv = max(mv, __shfl_xor_sync(0xffffffffu, mv, o));
+                mk = max(mk, __shfl_xor_sync(0xffffffffu, mk, o));
+            }
+            if (lane == 0) {
+                red_c[0] = mv;
+                red_c2[0] = mk;
+            }
         }
+        __syncthreads();
+        mv = red_c[0];
+        mk = red_c2[0];
         if (mv > kBucketMax && mk > kBucketMax) {
             __syncthreads();
             return false;
@@ -621,13 +648,13 @@ __device__ __forceinline__ bool rank_one_row_bucket(const T *__restrict__ row, T
             if (v[e] == v[e]) {
                 const int b = bk[e];
                 const int p0 = (int)hist[b], p1 = b + 1 < kBucketN ? (int)hist[b + 1] : n;
-                long long less = p0, eq = 0;
+                int less = p0, eq = 0;
                 for (int p = p0; p < p1; p++) {
                     const T y = vals[p];
                     less += (y < v[e]);
                     eq += (y == v[e]);
                 }
-                const long long start = less, end = less + eq;
+                const long long start = less, end = (long long)less + eq;
                 const long long rsum = (start + end + 1) * (end - start) / 2;
                 res = kdiv(kdiv((T)rsum, (T)(end - start)), (T)n);
             }
