@@ -548,15 +548,14 @@ def generate_module(spec: dict, out_dir: str, tag: str = None, stages_per_file: 
 #define KUN_TS_MINB 1
 #endif
 namespace kun {{
+// LogFast's tables in global memory (one 128- or 256-byte line each, read
+// through the cache): a table local to the function would be rebuilt in
+// local memory on every call
+__device__ const {T} kLogR[32] = {{{", ".join(r)}}};
+__device__ const {T} kLogLR[32] = {{{", ".join(lr)}}};
 template <> struct LogTables<{T}> {{
-  static __device__ __forceinline__ {T} r(unsigned long long i) {{
-    const {T} t[32] = {{{", ".join(r)}}};
-    return t[i];
-  }}
-  static __device__ __forceinline__ {T} lr(unsigned long long i) {{
-    const {T} t[32] = {{{", ".join(lr)}}};
-    return t[i];
-  }}
+  static __device__ __forceinline__ {T} r(unsigned long long i) {{ return kLogR[i]; }}
+  static __device__ __forceinline__ {T} lr(unsigned long long i) {{ return kLogLR[i]; }}
 }};
 }}  // namespace kun
 """
