@@ -433,10 +433,94 @@ extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
 }}
 """
 
+    def gen_generic(self) -> Tuple[str, str]:
+        """A GenericCrossSectionalOp: its head and body (C++ text over `T`,
+        `num_stocks`, `input_N[i]`, `output_N[i]`, KunQuant/ops/MiscOp.py:
+        201-224) compiled as device code, one thread per time row, each row
+        walking its stocks in order as the reference's stage loop does for
+        each time index (KunQuant/passes/CodegenCpp.py:107-138).  STs operands
+        go through [length][S] scratch like the other row kernels."""
+        ops, T = self.ops, self.T
+        xop = next(i for i, o in enumerate(ops) if o["k"] == "GenericCrossSectional")
+        ins = [ops[j] for j in ops[xop]["in"]]
+        outs = [o for o in ops if o["k"] == "Output"]
+        for o in ins:
+            if o["k"] != "Input":
+                raise RuntimeError("cross-sectional stage input must be a buffer")
+        for o in ins + outs:  # register every slot before sizing the slot array
+            self.slot(o["buf"])
+        nslots = len(self.slots)
+        pstruct = f"P_{self.kname}"
+        kern = f"kcs_{self.kname}"
+        L = self.blocking
+        pre, post, argin, argout = [], [], [], []
+        for k, o in enumerate(ins):
+            sl, user = self.slot(o["buf"]), self.is_user_input(o)
+            if self.layout_of(o) == "STs":
+                sc = len(self.scratch)
+                self.scratch[("in", k)] = sc
+                rows, row0 = ("P.total_time", "P.start") if user else ("P.length", "0")
+                pre.append(f"  if (int e = kun::launch_sts_to_ts<{T}>((const {T}*)P.p[{sl}], ({T}*)a->scratch[{sc}], "
+                           f"P.S, {rows}, {row0}, P.length, {L}, (cudaStream_t)stream)) return e;")
+                argin.append(f"(const {T}*)a->scratch[{sc}]")
+            else:
+                argin.append(f"(const {T}*)P.p[{sl}] + ({1 if user else 0} ? P.start : 0) * P.S")
+        for k, o in enumerate(outs):
+            sl = self.slot(o["buf"])
+            if self.layout_of(o) == "STs":
+                sc = len(self.scratch)
+                self.scratch[("out", k)] = sc
+                argout.append(f"({T}*)a->scratch[{sc}]")
+                post.append(f"  if (int e = kun::launch_ts_to_sts<{T}>(({T}*)a->scratch[{sc}], ({T}*)P.p[{sl}], "
+                            f"P.S, P.length, {L}, (cudaStream_t)stream)) return e;")
+            else:
+                argout.append(f"({T}*)P.p[{sl}]")
+        params = [f"const {T}* __restrict__ kun_in_{k}" for k in range(len(ins))] + \
+                 [f"{T}* __restrict__ kun_out_{k}" for k in range(len(outs))]
+        rows = [f"    const kun::CsRow<const {T}> input_{k}{{kun_in_{k} + kun_t * kun_S}};" for k in range(len(ins))] + \
+               [f"    const kun::CsRow<{T}> output_{k}{{kun_out_{k} + kun_t * kun_S}};" for k in range(len(outs))]
+        src = f"""
+struct {pstruct} {{
+  void* p[{nslots}];
+  long long S, total_time, start, length;
+}};
+__global__ void __launch_bounds__(128) {kern}({", ".join(params)}, long long kun_S, long long kun_length) {{
+  const long long kun_t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (kun_t >= kun_length) return;
+  using T = {T};
+  const size_t num_stocks = (size_t)kun_S;
+  (void)num_stocks;
+  // {ops[xop].get("op_class", "GenericCrossSectionalOp")}: generate_head()
+{ops[xop].get("head", "")}
+  {{
+{chr(10).join(rows)}
+    // generate_body()
+{ops[xop]["body"]}
+  }}
+}}
+"""
+        call = (f"  {kern}<<<(unsigned)((P.length + 127) / 128), 128, 0, (cudaStream_t)stream>>>("
+                f"{', '.join(argin + argout)}, P.S, P.length);\n"
+                f"  if (int e = (int)cudaGetLastError()) return e;")
+        fill = "\n".join(f"  P.p[{sl}] = a->buffers[{bid}];" for bid, sl in self.slots.items())
+        body = "\n".join(pre + [call] + post + ["  return 0;"])
+        launch = f"""
+extern "C" int {self.kname}_launch(const KunGpuStageArgs* a, void* stream) {{
+  {pstruct} P;
+{fill}
+  P.S = a->num_stocks; P.total_time = a->total_time; P.start = a->start; P.length = a->length;
+  if (a->num_stocks <= 0 || a->length <= 0) return 0;
+{body}
+}}
+"""
+        return src, launch
+
     def gen_xsec(self) -> Tuple[str, str]:
         ops = self.ops
         T = self.T
         kind = self.st["kind"]
+        if kind == "generic":
+            return self.gen_generic()
         xop = next(i for i, o in enumerate(ops) if o["k"] in ("Rank", "Scale", "DiffWithWeightedSum"))
         ins = [ops[j] for j in ops[xop]["in"]]
         outop = next(o for o in ops if o["k"] == "Output")
@@ -616,7 +700,7 @@ template <> struct LogTables<{T}> {{
             arr = ", ".join(str(v) for v in vals) if vals else "-1"
             lines.append(f"static const int32_t st{si}_{key}[] = {{{arr}}};")
     kinds = {"ts": "KUN_STAGE_TS", "rank": "KUN_STAGE_RANK", "scale": "KUN_STAGE_SCALE",
-             "xsec": "KUN_STAGE_XSEC"}
+             "xsec": "KUN_STAGE_XSEC", "generic": "KUN_STAGE_XSEC"}
     lines.append(f"static const KunGpuStageDesc stages_{tag}[] = {{")
     for si, st in enumerate(spec["stages"]):
         lines.append(f"  {{{_c_str(st['name'][:200])}, {kinds[st['kind']]}, {len(st['in'])}, st{si}_in, "

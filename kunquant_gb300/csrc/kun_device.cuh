@@ -456,6 +456,11 @@ template <typename T, bool IsMax, bool IsArg> struct RExt {
         return v == (IsMax ? -kinf<T>() : kinf<T>()) ? T(0) : ksub(row, pos);
     }
 };
+// row accessor of a GenericCrossSectionalOp body: input_N[i], output_N[i]
+template <typename T> struct CsRow {
+    T *p;
+    __device__ __forceinline__ T &operator[](size_t i) const { return p[i]; }
+};
 template <typename T> struct RVal {
     T v;
     __device__ __forceinline__ T value() const { return v; }

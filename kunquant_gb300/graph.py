@@ -54,8 +54,22 @@ def _value_text(v) -> str:
     return str(v)
 
 
+def _generic_cross_sectional(op) -> bool:
+    """A GenericCrossSectionalOp with its own C++ body
+    (``KunQuant/ops/MiscOp.py:201-224``); DiffWithWeightedSum has a row kernel
+    of its own."""
+    from KunQuant.ops.MiscOp import GenericCrossSectionalOp
+    return isinstance(op, GenericCrossSectionalOp) and op.__class__.__name__ != "DiffWithWeightedSum"
+
+
 def _encode_op(op, f, bufid_of_name: Dict[str, int], stream_temp_bufs: Dict[int, int]):
     name = op.__class__.__name__
+    if _generic_cross_sectional(op):
+        # the body runs as device code, one thread per time row, over the
+        # stocks in order, as the reference's stage loop runs it per row
+        # (KunQuant/passes/CodegenCpp.py:107-138)
+        return {"k": "GenericCrossSectional", "op_class": name, "in": [f.get_op_idx(i) for i in op.inputs],
+                "p": -1, "head": op.generate_head(), "body": op.generate_body()}
     if name not in SUPPORTED:
         raise RuntimeError(f"op {name} is not supported by the GPU backend: {op}")
     d = {"k": name, "in": [f.get_op_idx(i) for i in op.inputs]}
@@ -97,6 +111,8 @@ def _stage_kind(f) -> str:
             return "scale"
         if n == "DiffWithWeightedSum":
             return "xsec"
+        if _generic_cross_sectional(op):
+            return "generic"
     return "ts"
 
 

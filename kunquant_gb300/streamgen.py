@@ -381,6 +381,9 @@ extern "C" int {self.kname}_init(const KunGpuStageArgs* a, void* stream) {{
     def gen_xsec(self):
         ops, T = self.ops, self.T
         kind = self.st["kind"]
+        if kind == "generic":
+            raise RuntimeError("a GenericCrossSectionalOp with its own C++ body is supported in batch "
+                               "mode only, not in stream mode")
         xop = next(i for i, o in enumerate(ops) if o["k"] in ("Rank", "Scale", "DiffWithWeightedSum"))
         ins = [ops[j] for j in ops[xop]["in"]]
         outop = next(o for o in ops if o["k"] == "Output")

@@ -230,6 +230,9 @@ def contraction_plan(ops):
 
 
 def _encode_stage(spec, st):
+    if st["kind"] == "generic":
+        raise NotImplementedError("the oracle does not run GenericCrossSectionalOp C++ bodies; "
+                                  "their parity is pinned on the reference's own outputs")
     ops = st["ops"]
     arr = (KOOp * len(ops))()
     fplan = contraction_plan(ops) if st["kind"] == "ts" else {}

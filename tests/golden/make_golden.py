@@ -161,6 +161,77 @@ def _graphs():
     }
 
 
+def _generic_graphs():
+    """GenericCrossSectionalOp subclasses with their own C++ bodies
+    (KunQuant/ops/MiscOp.py:201-224): the reference compiles the body into its
+    stage function; the GPU backend compiles the same text as device code.
+    Sums in stock order and one IEEE division, so the bits must agree."""
+    from KunQuant.Op import Builder, Input, Output
+    from KunQuant.ops.MiscOp import GenericCrossSectionalOp
+    from KunQuant.Stage import Function
+
+    class NanDemean(GenericCrossSectionalOp):
+        """x minus the mean of the row's numbers (NaN cells skipped)"""
+
+        def __init__(self, v):
+            super().__init__([v], None)
+
+        def generate_head(self):
+            return "    const T kZero = 0;"
+
+        def generate_body(self):
+            return """
+        T sum = kZero;
+        size_t n = 0;
+        for (size_t i = 0; i < num_stocks; i++) {
+            T v = input_0[i];
+            if (v == v) {
+                sum += v;
+                n++;
+            }
+        }
+        T mean = sum / (T)n;
+        for (size_t i = 0; i < num_stocks; i++) {
+            output_0[i] = input_0[i] - mean;
+        }
+        """
+
+    class RatioToRowMax(GenericCrossSectionalOp):
+        """a over the row's largest b (NaN cells skipped)"""
+
+        def __init__(self, a, b):
+            super().__init__([a, b], None)
+
+        def generate_head(self):
+            return ""
+
+        def generate_body(self):
+            return """
+        T mx = (T)(-1e30);
+        for (size_t i = 0; i < num_stocks; i++) {
+            T v = input_1[i];
+            if (v > mx) mx = v;
+        }
+        for (size_t i = 0; i < num_stocks; i++) {
+            output_0[i] = input_0[i] / mx;
+        }
+        """
+
+    def build():
+        bld = Builder()
+        with bld:
+            a, c = Input("a"), Input("b")
+            Output(NanDemean(a), "demean")
+            Output(RatioToRowMax(a * 2, c), "ratio")
+            Output(NanDemean(a - c) + a, "mixed")
+        return Function(bld.ops)
+
+    return {
+        "generic_cs_f32": (build, dict(input_layout="TS", output_layout="TS"), "ab"),
+        "generic_cs_sts_f32": (build, dict(input_layout="STs", output_layout="STs"), "ab_sts"),
+    }
+
+
 def _inputs(kind, dtype):
     rng = np.random.default_rng(2024)
     if kind == "issue19":
@@ -349,6 +420,13 @@ def main(names):
               {"stream": True, "ticks": ticks})
     if not names or any(n.startswith("util_") for n in names):
         _utilities()
+    for name, (build, cfg, kind) in _generic_graphs().items():
+        if names and name not in names:
+            continue
+        spec, mod = refkun.compile_function("g_" + name, build, name, **cfg)
+        dt = np.float32 if spec["dtype"] == "float" else np.float64
+        inputs = _inputs(kind, dt)
+        _save(name, spec, inputs, refkun.run_module(mod, inputs), {"generic_cs": True})
     for name, (build, cfg, kind) in _graphs().items():
         if names and name not in names:
             continue

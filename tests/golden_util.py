@@ -47,6 +47,13 @@ def is_utility(name):
         return "utility" in json.loads(f.read())["spec"]
 
 
+def is_generic(name):
+    """Fixtures of GenericCrossSectionalOp subclasses with their own C++
+    bodies: pinned on the reference's outputs; the oracle does not run them."""
+    with gzip.open(os.path.join(GOLDEN, name + ".json.gz"), "rb") as f:
+        return bool(json.loads(f.read()).get("generic_cs"))
+
+
 def num_time(inputs):
     """Rows of a fixture's inputs: [T][S] or STs [S/L][T][L]."""
     a = next(iter(inputs.values()))

@@ -45,7 +45,7 @@ def rank_amplified(name):
     return _lookup(RANK_AMPLIFIED, name)
 
 
-BATCH = [n for n in G.names() if not G.is_stream(n) and not G.is_utility(n)]
+BATCH = [n for n in G.names() if not G.is_stream(n) and not G.is_utility(n) and not G.is_generic(n)]
 
 
 def check_against_reference(name, got, ref, meta):
