@@ -86,3 +86,34 @@ def test_launch_struct_holds_every_slot(name, tmp_path):
         n = sizes[m.group(2)]
         used = [int(k) for k in re.findall(r"P\.p\[(\d+)\] = ", m.group(3))]
         assert all(k < n for k in used), (m.group(1), n, used)
+
+
+def test_stream_mode_refuses_generic_bodies(tmp_path):
+    """Stream modules refuse a GenericCrossSectionalOp body at code
+    generation, with a message (needs KunQuant's front end)."""
+    try:
+        from kunquant_gb300.graphs import export_predefined
+        export_predefined._front_end()
+        from KunQuant.Op import Builder, Input, Output
+        from KunQuant.ops.MiscOp import GenericCrossSectionalOp
+        from KunQuant.Stage import Function
+    except Exception:
+        pytest.skip("KunQuant front end not importable")
+    from kunquant_gb300.graph import export_function
+
+    class Copy(GenericCrossSectionalOp):
+        def __init__(self, v):
+            super().__init__([v], None)
+
+        def generate_head(self):
+            return ""
+
+        def generate_body(self):
+            return "for (size_t i = 0; i < num_stocks; i++) output_0[i] = input_0[i];"
+
+    b = Builder()
+    with b:
+        Output(Copy(Input("a")), "out")
+    spec = export_function(Function(b.ops), "gen_stream", input_layout="STREAM", output_layout="STREAM")
+    with pytest.raises(RuntimeError, match="stream mode"):
+        codegen.generate_module(spec, str(tmp_path), tag="gen_stream")
