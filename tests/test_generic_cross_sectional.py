@@ -70,7 +70,7 @@ def test_gpu_matches_reference(name):
     assert not compare_exact(got, ref)
 
 
-@pytest.mark.parametrize("name", CASES + ["misc_f32", "rank029_f64", "stats_sts_f32"])
+@pytest.mark.parametrize("name", CASES + ["misc_f32", "rank029_f64", "stats_sts_f32", "alpha158_f32", "alpha101_f32"])
 def test_launch_struct_holds_every_slot(name, tmp_path):
     """Every stage launcher fills P.p[k] only for k below the size of its
     struct's slot array."""
